@@ -1,0 +1,82 @@
+"""Build the GB300 library in-tree: generate the class kernels, compile every
+translation unit with nvcc for sm_103a in parallel, link one shared library.
+
+Output: fock-rs_gb300/lib/libfock_gb300.so  (C ABI of include/fock_gb300.h)
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+GEN = os.path.join(CSRC, "gen")
+OBJ = os.path.join(HERE, "_build")
+LIBDIR = os.path.join(HERE, "lib")
+LIB = os.path.join(LIBDIR, "libfock_gb300.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+LMAX = int(os.environ.get("FOCK_GB300_LMAX", "2"))
+
+
+def nvcc():
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return cand
+
+
+def _sources():
+    srcs = [os.path.join(CSRC, f) for f in ("fock_api.cu", "md_device.cu", "scf_device.cu")]
+    srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("inst_") and f.endswith(".cu"))
+    return srcs
+
+
+def _deps_mtime():
+    m = 0.0
+    for root in (CSRC, GEN, os.path.join(os.path.dirname(HERE), "include")):
+        for f in os.listdir(root):
+            p = os.path.join(root, f)
+            if os.path.isfile(p) and f.endswith((".cu", ".cuh", ".h", ".py")):
+                m = max(m, os.path.getmtime(p))
+    return m
+
+
+def _compile(src, verbose):
+    obj = os.path.join(OBJ, os.path.basename(src) + ".o")
+    if os.path.exists(obj) and os.path.getmtime(obj) >= _deps_mtime():
+        return obj
+    cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj,
+                             "-I", CSRC, "--expt-relaxed-constexpr"]
+    if verbose:
+        cmd += ["-Xptxas", "-v"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("nvcc failed for %s:\n%s\n%s" % (src, r.stdout, r.stderr))
+    if verbose:
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build(verbose=False, jobs=None):
+    sys.path.insert(0, CSRC)
+    import gen_eri  # noqa
+    sys.path.pop(0)
+    os.makedirs(GEN, exist_ok=True)
+    gen_eri.main(GEN, LMAX)
+    os.makedirs(OBJ, exist_ok=True)
+    os.makedirs(LIBDIR, exist_ok=True)
+    srcs = _sources()
+    jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = list(ex.map(lambda s: _compile(s, verbose), srcs))
+    cuda_lib = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "lib64")
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + [
+        "-L", cuda_lib, "-lcublas", "-lcusolver", "-Xlinker", "-rpath=" + cuda_lib]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n%s\n%s" % (r.stdout, r.stderr))
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,302 @@
+// ERI + J/K digestion kernel template, one instantiation per angular class.
+//
+// Work mapping (MODE_JK / MODE_TENSOR): one warp = one bra shell pair and up
+// to 32 ket shell pairs of the same (row) list; one lane = one contracted
+// shell quartet.  The bra is uniform across the warp, so its primitive loop
+// has a uniform trip count and its J block is reduced with warp shuffles
+// before a single set of atomics.  Every lane runs Obara-Saika VRR over the
+// bra x ket primitive pairs into contracted [e0|f0] accumulators held in
+// registers, then HRR once per contracted quartet, then digests the
+// integrals straight into the Fock accumulator M (G = M + M^T): the N^4
+// tensor is never stored.
+//
+// Digestion of one integral v = (ij|kl) with degeneracy factor s (1/2 for
+// each of a==b, c==d, ab==cd) follows from the eight index images of v:
+//   M_ij += 2 s v D_kl     M_kl += 2 s v D_ij
+//   M_ik -= s v D_jl / 2   M_jl -= s v D_ik / 2
+//   M_il -= s v D_jk / 2   M_jk -= s v D_il / 2
+// which gives G = J - K/2 = M + M^T for a symmetric density.
+#pragma once
+#include "common.cuh"
+#include "gen/eri_classes.cuh"
+
+namespace fockgb {
+
+constexpr int kEriThreads = 128;
+
+template <typename R>
+struct PrimLoad;
+
+template <>
+struct PrimLoad<double> {
+  double p, o2p, K, P[3], PA[3];
+  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
+    const double2* v = a.prim64[idx].v;
+    double2 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2), v3 = __ldg(v + 3), v4 = __ldg(v + 4);
+    p = v0.x; o2p = v0.y; K = v1.x; P[0] = v1.y; P[1] = v2.x; P[2] = v2.y;
+    PA[0] = v3.x; PA[1] = v3.y; PA[2] = v4.x;
+  }
+};
+
+template <>
+struct PrimLoad<float> {
+  float p, o2p, K, P[3], PA[3];
+  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
+    const float4* v = a.prim32[idx].v;
+    float4 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2);
+    p = v0.x; o2p = v0.y; K = v0.z; P[0] = v0.w; P[1] = v1.x; P[2] = v1.y;
+    PA[0] = v1.z; PA[1] = v1.w; PA[2] = v2.x;
+  }
+};
+
+template <typename R>
+__device__ __forceinline__ const R* boys_table(const EriArgs& a);
+template <>
+__device__ __forceinline__ const double* boys_table<double>(const EriArgs& a) { return a.boys64; }
+template <>
+__device__ __forceinline__ const float* boys_table<float>(const EriArgs& a) { return a.boys32; }
+
+template <typename R>
+__device__ __forceinline__ R dens(const EriArgs& a, int i, int j);
+template <>
+__device__ __forceinline__ double dens<double>(const EriArgs& a, int i, int j) { return __ldg(a.D + (size_t)i * a.nbf + j); }
+template <>
+__device__ __forceinline__ float dens<float>(const EriArgs& a, int i, int j) { return __ldg(a.D32 + (size_t)i * a.nbf + j); }
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class C, typename R, int MODE>
+__global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, const EriArgs a) {
+  constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, NE = C::NE, NF = C::NF, L = C::L;
+  const int lane = threadIdx.x & 31;
+  int bra, ket;
+  bool active;
+  if (MODE == MODE_SCHWARZ) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    active = t < cl.nrows;
+    bra = ket = cl.bra_list[active ? t : 0];
+  } else {
+    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (gw >= cl.nwarps) return;  // uniform per warp
+    int lo = 0, hi = cl.nrows - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(cl.row_warp_off + mid) <= gw) lo = mid; else hi = mid - 1;
+    }
+    const int k = (int)(gw - __ldg(cl.row_warp_off + lo)) * 32 + lane;
+    const int cnt = __ldg(cl.row_cnt + lo);
+    active = k < cnt;
+    bra = __ldg(cl.bra_list + lo);
+    ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + (active ? k : 0));
+  }
+  const PairInfo& Pb = a.pairs[bra];
+  const PairInfo& Pk = a.pairs[ket];
+  const int nbp = Pb.nprim;
+  const int nkp = active ? Pk.nprim : 0;
+  const int bp0 = Pb.prim_off, kp0 = Pk.prim_off;
+
+  R acc[NE * NF];
+#pragma unroll
+  for (int i = 0; i < NE * NF; ++i) acc[i] = R(0);
+
+  const R* btab = boys_table<R>(a);
+  for (int ib = 0; ib < nbp; ++ib) {
+    PrimLoad<R> bp;
+    bp.load(a, bp0 + ib);
+    for (int ik = 0; ik < nkp; ++ik) {
+      PrimLoad<R> kp;
+      kp.load(a, kp0 + ik);
+      const R s = bp.p + kp.p;
+      const R rs = rsqrt_r<R>(s);
+      const R inv = rs * rs;
+      const R rp = kp.p * inv;   // rho / p
+      const R rq = bp.p * inv;   // rho / q
+      const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
+      const R r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
+      const R T = kp.p * rp * r2;  // rho |PQ|^2
+      const R pref = bp.K * kp.K * rs;
+      R F[L + 1];
+      boys_scaled<L>(T, pref, btab, a.exp64, F);
+      const R WP[3] = {-rp * PQ[0], -rp * PQ[1], -rp * PQ[2]};
+      const R WQ[3] = {rq * PQ[0], rq * PQ[1], rq * PQ[2]};
+      const R o2pq = R(0.5) * inv;
+      C::template vrr<R>(F, bp.PA, WP, kp.PA, WQ, bp.o2p, kp.o2p, o2pq, rp, rq, acc);
+    }
+  }
+
+  R AB[3], CD[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) { AB[i] = (R)Pb.AB[i]; CD[i] = (R)Pk.AB[i]; }
+  R out[NA * NB * NC * ND];
+  C::template hrr<R>(acc, AB, CD, out);
+  if (C::LA >= 2 || C::LB >= 2 || C::LC >= 2 || C::LD >= 2) {
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+          for (int id = 0; id < ND; ++id)
+            out[((ia * NB + ib) * NC + ic) * ND + id] *=
+                (R)(comp_factor(C::LA, ia) * comp_factor(C::LB, ib) * comp_factor(C::LC, ic) * comp_factor(C::LD, id));
+  }
+
+  const int fa = Pb.fa, fb = Pb.fb, fc = Pk.fa, fd = Pk.fb;
+  if (MODE == MODE_SCHWARZ) {
+    if (!active) return;
+    double q = 0.0;
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib) {
+        double v = fabs((double)out[((ia * NB + ib) * NC + ia) * ND + ib]);
+        q = v > q ? v : q;
+      }
+    a.schwarz[bra] = (float)sqrt(q);
+    return;
+  }
+  if (MODE == MODE_TENSOR) {
+    if (!active) return;
+    const size_t n = (size_t)a.nbf;
+#pragma unroll 1
+    for (int ia = 0; ia < NA; ++ia)
+      for (int ib = 0; ib < NB; ++ib)
+        for (int ic = 0; ic < NC; ++ic)
+          for (int id = 0; id < ND; ++id) {
+            const double v = (double)out[((ia * NB + ib) * NC + ic) * ND + id];
+            const size_t i = fa + ia, j = fb + ib, k = fc + ic, l = fd + id;
+            a.tensor[((l * n + k) * n + j) * n + i] = v;
+            a.tensor[((l * n + k) * n + i) * n + j] = v;
+            a.tensor[((k * n + l) * n + j) * n + i] = v;
+            a.tensor[((k * n + l) * n + i) * n + j] = v;
+            a.tensor[((j * n + i) * n + l) * n + k] = v;
+            a.tensor[((j * n + i) * n + k) * n + l] = v;
+            a.tensor[((i * n + j) * n + l) * n + k] = v;
+            a.tensor[((i * n + j) * n + k) * n + l] = v;
+          }
+    return;
+  }
+
+  // ---- MODE_JK: fused digestion ----
+  R jab[NA * NB], jcd[NC * ND], kac[NA * NC], kad[NA * ND], kbc[NB * NC], kbd[NB * ND];
+#pragma unroll
+  for (int i = 0; i < NA * NB; ++i) jab[i] = R(0);
+  if (active) {
+    R Dab[NA * NB], Dcd[NC * ND], Dac[NA * NC], Dad[NA * ND], Dbc[NB * NC], Dbd[NB * ND];
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = dens<R>(a, fa + ia, fb + ib);
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+      for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = dens<R>(a, fc + ic, fd + id);
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia) {
+#pragma unroll
+      for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = dens<R>(a, fa + ia, fc + ic);
+#pragma unroll
+      for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = dens<R>(a, fa + ia, fd + id);
+    }
+#pragma unroll
+    for (int ib = 0; ib < NB; ++ib) {
+#pragma unroll
+      for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = dens<R>(a, fb + ib, fc + ic);
+#pragma unroll
+      for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = dens<R>(a, fb + ib, fd + id);
+    }
+#pragma unroll
+    for (int i = 0; i < NC * ND; ++i) jcd[i] = R(0);
+#pragma unroll
+    for (int i = 0; i < NA * NC; ++i) kac[i] = R(0);
+#pragma unroll
+    for (int i = 0; i < NA * ND; ++i) kad[i] = R(0);
+#pragma unroll
+    for (int i = 0; i < NB * NC; ++i) kbc[i] = R(0);
+#pragma unroll
+    for (int i = 0; i < NB * ND; ++i) kbd[i] = R(0);
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+          for (int id = 0; id < ND; ++id) {
+            const R v = out[((ia * NB + ib) * NC + ic) * ND + id];
+            jab[ia * NB + ib] += v * Dcd[ic * ND + id];
+            jcd[ic * ND + id] += v * Dab[ia * NB + ib];
+            kac[ia * NC + ic] += v * Dbd[ib * ND + id];
+            kbd[ib * ND + id] += v * Dac[ia * NC + ic];
+            kad[ia * ND + id] += v * Dbc[ib * NC + ic];
+            kbc[ib * NC + ic] += v * Dad[ia * ND + id];
+          }
+  }
+  const double sdeg = (Pb.sa == Pb.sb ? 0.5 : 1.0) * (Pk.sa == Pk.sb ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
+  const double sj = 2.0 * sdeg, sk = -0.5 * sdeg;
+  const size_t n = (size_t)a.nbf;
+  // bra J block: identical bra across the warp -> shuffle-reduce, one atomic per element
+#pragma unroll
+  for (int i = 0; i < NA * NB; ++i) {
+    double v = (double)jab[i] * (active ? sj : 0.0);
+    v = warp_sum(v);
+    if (lane == 0 && v != 0.0) atomicAdd(a.M + (size_t)(fa + i / NB) * n + (fb + i % NB), v);
+  }
+  if (!active) return;
+#pragma unroll
+  for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fc + ic) * n + (fd + id), sj * (double)jcd[ic * ND + id]);
+#pragma unroll
+  for (int ia = 0; ia < NA; ++ia) {
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + (size_t)(fa + ia) * n + (fc + ic), sk * (double)kac[ia * NC + ic]);
+#pragma unroll
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fa + ia) * n + (fd + id), sk * (double)kad[ia * ND + id]);
+  }
+#pragma unroll
+  for (int ib = 0; ib < NB; ++ib) {
+#pragma unroll
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + (size_t)(fb + ib) * n + (fc + ic), sk * (double)kbc[ib * NC + ic]);
+#pragma unroll
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fb + ib) * n + (fd + id), sk * (double)kbd[ib * ND + id]);
+  }
+}
+
+template <class C>
+cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if (mode == MODE_SCHWARZ) {
+    if (cl.nrows <= 0) return cudaSuccess;
+    if constexpr (C::LA == C::LC && C::LB == C::LD) {
+      const int blocks = (cl.nrows + kEriThreads - 1) / kEriThreads;
+      eri_kernel<C, double, MODE_SCHWARZ><<<blocks, kEriThreads, 0, s>>>(cl, a);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorInvalidValue;
+    }
+  }
+  if (cl.nwarps <= 0) return cudaSuccess;
+  const long long threads = cl.nwarps * 32;
+  const long long blocks = (threads + kEriThreads - 1) / kEriThreads;
+  if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  if (mode == MODE_TENSOR) {
+    eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+  } else if (prec == PREC_FP32) {
+    eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+  } else {
+    eri_kernel<C, double, MODE_JK><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace fockgb

@@ -1,0 +1,1053 @@
+// Host side of the GB300 ERI + Fock library: the C ABI of include/fock_gb300.h.
+//
+//   fock_ctx_create   shells -> normalised primitives -> shell pairs and
+//                     primitive-pair data -> Schwarz factors (device) ->
+//                     class-sorted quartet plans (device lists)
+//   fock_build_jk     fused ERI + J/K on the device (eri_kernel.cuh)
+//   fock_eri_tensor   full N^4 tensor (debug / parity)
+//   fock_scf          RHF with device-resident FP64 linear algebra
+//
+// Reference interfaces replaced: ElectronTensor::from_basis
+// (basis/src/electron_tensor.rs:81-176), the Fock build of try_scf
+// (scf/src/lib.rs:167-187) and try_scf itself (scf/src/lib.rs:73-258).
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/fock_gb300.h"
+#include "common.cuh"
+#include "gen/dispatch.cuh"
+#include "md_device.cuh"
+#include "scf_device.cuh"
+
+using namespace fockgb;
+
+namespace {
+
+constexpr int kMaxL = 2;
+constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
+
+inline int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
+inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
+
+// ---------------------------------------------------------------------------
+// Boys tables (host generation, once per process).
+// F_n(T_i), T_i = i/16, from the power series
+//   F_n(T) = e^{-T} sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1))
+// (positive terms, no cancellation) for the top order in long double, then
+// the stable downward recursion F_{n-1} = (2T F_n + e^{-T}) / (2n-1).
+// ---------------------------------------------------------------------------
+constexpr int kTabOrders = kBoysMaxM + kBoysTerms;  // F_0 .. F_{M+7}
+std::once_flag g_tab_once;
+std::vector<double> g_boys64, g_exp64, g_ref_lut;
+std::vector<float> g_boys32;
+
+long double boys_series_ld(int n, long double T) {
+  long double term = 1.0L / (2 * n + 1), sum = term;
+  for (int k = 1; k < 2000; ++k) {
+    term *= 2.0L * T / (2 * n + 2 * k + 1);
+    sum += term;
+    if (term < 1e-24L * sum) break;
+  }
+  return expl(-T) * sum;
+}
+
+void build_tables() {
+  std::vector<long double> F((size_t)kBoysPts * (kTabOrders + 1));
+  for (int i = 0; i < kBoysPts; ++i) {
+    const long double T = (long double)i / 16.0L;
+    const long double e = expl(-T);
+    long double f = boys_series_ld(kTabOrders, T);
+    F[(size_t)i * (kTabOrders + 1) + kTabOrders] = f;
+    for (int n = kTabOrders; n > 0; --n) {
+      f = (2.0L * T * f + e) / (2 * n - 1);
+      F[(size_t)i * (kTabOrders + 1) + n - 1] = f;
+    }
+  }
+  g_boys64.assign((size_t)(kBoysMaxM + 1) * kBoysPts * kBoysTerms, 0.0);
+  g_boys32.assign(g_boys64.size(), 0.0f);
+  g_exp64.resize(kBoysPts);
+  for (int M = 0; M <= kBoysMaxM; ++M)
+    for (int i = 0; i < kBoysPts; ++i) {
+      long double fact = 1.0L;
+      for (int k = 0; k < kBoysTerms; ++k) {
+        if (k > 0) fact *= k;
+        long double c = F[(size_t)i * (kTabOrders + 1) + M + k] / fact;
+        if (k & 1) c = -c;
+        const size_t idx = ((size_t)M * kBoysPts + i) * kBoysTerms + k;
+        g_boys64[idx] = (double)c;
+        g_boys32[idx] = (float)c;
+      }
+    }
+  for (int i = 0; i < kBoysPts; ++i) g_exp64[i] = (double)expl(-(long double)i / 16.0L);
+  // reference LUT: F_10(0.15 k), k < 200 (boys/src/lut.rs values, regenerated)
+  g_ref_lut.resize(200);
+  for (int k = 0; k < 200; ++k) g_ref_lut[k] = (double)boys_series_ld(10, (long double)((double)k * 0.15));
+}
+
+// reference normalisation of a Cartesian primitive (basis/src/primitives.rs:19-27)
+double prim_norm(int i, int j, int k, double alpha) {
+  auto pr = [](int lo, int hi) { long long r = 1; for (int q = lo; q <= hi; ++q) r *= q; return r; };
+  const double a = std::sqrt(std::sqrt(std::pow(M_2_PI * alpha, 3)));
+  const long long den = pr(i + 1, 2 * i) * pr(j + 1, 2 * j) * pr(k + 1, 2 * k);
+  return a * std::sqrt(std::pow(8.0 * alpha, i + j + k) / (double)den);
+}
+
+struct HostShell {
+  int l, atom, nprim, f0;
+  double c[3];
+  std::vector<double> exps, coefs;  // coefs normalised for the x^l component
+};
+
+struct Plan {
+  int la, lb, lc, ld, prec;
+  ClassLaunch cl;
+  long long quartets, prim_quartets;
+};
+
+int map_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return FOCK_OK;
+  if (e == cudaErrorMemoryAllocation) return FOCK_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return FOCK_ERR_NO_DEVICE;
+  return FOCK_ERR_CUDA;
+}
+
+#define CK(x)                                   \
+  do {                                          \
+    cudaError_t _e = (x);                       \
+    if (_e != cudaSuccess) return map_cuda(_e); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(T** p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void**)p, n * sizeof(T));
+}
+
+template <typename T>
+void dfree(T*& p) {
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+}  // namespace
+
+struct fock_ctx {
+  fock_options opt;
+  int device = 0;
+  int natom = 0, nbf = 0;
+  std::vector<fock_atom> atoms;
+  std::vector<HostShell> shells;
+  std::vector<double> fsign;  // (-1)^l per function (reference <-> textbook)
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  long long launches = 0;
+  // pairs
+  std::vector<PairInfo> hpairs;
+  std::vector<int> pair_nprim;
+  long long nprim_pairs = 0;
+  PairInfo* d_pairs = nullptr;
+  PrimPair64* d_prim64 = nullptr;
+  PrimPair32* d_prim32 = nullptr;
+  double *d_boys64 = nullptr, *d_exp64 = nullptr, *d_ref_lut = nullptr;
+  float* d_boys32 = nullptr;
+  float* d_schwarz = nullptr;
+  std::vector<float> Q;
+  // density / Fock buffers
+  double *d_D = nullptr, *d_M = nullptr, *d_G = nullptr;
+  float* d_D32 = nullptr;
+  // plans
+  std::vector<Plan> plans;
+  int* d_plan_int = nullptr;
+  long long* d_plan_ll = nullptr;
+  fock_stats stats{};
+  // MD basis (one-electron, refcompat tensor)
+  MdFunc* d_mdfuncs = nullptr;
+  double *d_mdexps = nullptr, *d_mdcoefs = nullptr, *d_atoms4 = nullptr;
+  // dense tensor (refcompat SCF)
+  double* d_tensor = nullptr;
+  // SCF library handles
+  cublasHandle_t blas = nullptr;
+  cusolverDnHandle_t solver = nullptr;
+};
+
+namespace {
+
+EriArgs eri_args(fock_ctx* c) {
+  EriArgs a{};
+  a.pairs = c->d_pairs;
+  a.prim64 = c->d_prim64;
+  a.prim32 = c->d_prim32;
+  a.boys64 = c->d_boys64;
+  a.exp64 = c->d_exp64;
+  a.boys32 = c->d_boys32;
+  a.D = c->d_D;
+  a.D32 = c->d_D32;
+  a.M = c->d_M;
+  a.tensor = nullptr;
+  a.schwarz = c->d_schwarz;
+  a.nbf = c->nbf;
+  return a;
+}
+
+MdBasis md_basis(fock_ctx* c) {
+  MdBasis b;
+  b.funcs = c->d_mdfuncs;
+  b.exps = c->d_mdexps;
+  b.coefs = c->d_mdcoefs;
+  b.nfunc = c->nbf;
+  return b;
+}
+
+MdTables md_tables(fock_ctx* c) {
+  MdTables t;
+  t.boys64 = c->d_boys64;
+  t.exp64 = c->d_exp64;
+  t.ref_lut = c->d_ref_lut;
+  return t;
+}
+
+// Per-primitive-quartet flops outside the generated VRR: pair setup
+// (s, rsqrt, 1/s, rho/p, rho/q, PQ, |PQ|^2, T, prefactor, WP, WQ, 1/(2(p+q)))
+// and the Boys evaluation of kernel common.cuh (FMA = 2 flops).
+long long setup_flops(int L) {
+  long long f = 32;
+  if (L <= 1) f += (L + 1) * 15 + 2;
+  else f += 14 + 15 + 2 + 3LL * L + (L + 1);
+  return f;
+}
+
+int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
+
+// Build the quartet plans from the Schwarz factors.
+int build_plan(fock_ctx* c, bool for_tensor) {
+  dfree(c->d_plan_int);
+  dfree(c->d_plan_ll);
+  c->plans.clear();
+  const double tau = for_tensor ? 0.0 : c->opt.schwarz_eps;
+  const bool mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
+  const double tmix = c->opt.mixed_threshold;
+  const int npairs = (int)c->hpairs.size();
+  // pairs per class, sorted by Q descending (ties by index for determinism)
+  std::vector<std::vector<int>> cls(kNumPairClasses);
+  for (int p = 0; p < npairs; ++p)
+    if (c->hpairs[p].nprim > 0) cls[c->hpairs[p].cls].push_back(p);
+  std::vector<int> rank(npairs, -1);
+  for (auto& v : cls) {
+    std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return c->Q[a] > c->Q[b]; });
+    for (size_t r = 0; r < v.size(); ++r) rank[v[r]] = (int)r;
+  }
+  std::vector<int> ints;
+  std::vector<long long> lls;
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, off; };
+  std::vector<Pending> pend;
+  fock_stats st{};
+  st.shell_pairs = npairs;
+  st.prim_pairs = c->nprim_pairs;
+  const long long nfp = (long long)c->nbf * (c->nbf + 1) / 2;
+  st.function_quartets_unique = nfp * (nfp + 1) / 2;
+  long long total_shell_quartets = 0;
+  for (int X = 0; X < kNumPairClasses; ++X) {
+    if (cls[X].empty()) continue;
+    for (int Y = 0; Y <= X; ++Y) {
+      if (cls[Y].empty()) continue;
+      int la = 0, lb = 0, lc = 0, ld = 0;
+      for (int a = 0; a <= kMaxL; ++a)
+        for (int b = 0; b <= a; ++b) {
+          if (pair_class(a, b) == X) { la = a; lb = b; }
+          if (pair_class(a, b) == Y) { lc = a; ld = b; }
+        }
+      const std::vector<int>& bras = cls[X];
+      const std::vector<int>& kall = cls[Y];
+      total_shell_quartets += (X == Y) ? (long long)bras.size() * (bras.size() + 1) / 2
+                                       : (long long)bras.size() * kall.size();
+      // ket groups (by primitive-pair count) keep the Q order
+      std::vector<std::vector<int>> groups;
+      if (c->opt.group_by_contraction) {
+        std::vector<int> keys;
+        for (int p : kall) keys.push_back(c->hpairs[p].nprim);
+        std::sort(keys.begin(), keys.end());
+        keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+        for (int k : keys) {
+          std::vector<int> g;
+          for (int p : kall) if (c->hpairs[p].nprim == k) g.push_back(p);
+          groups.push_back(g);
+        }
+      } else {
+        groups.push_back(kall);
+      }
+      int hrr = 0, neri = 0;
+      const int vrr = class_vrr_flops(la, lb, lc, ld, &hrr, &neri);
+      const int L = la + lb + lc + ld;
+      for (auto& g : groups) {
+        std::vector<float> gq(g.size());
+        std::vector<int> grank(g.size());
+        std::vector<long long> gprim(g.size() + 1, 0);
+        for (size_t k = 0; k < g.size(); ++k) {
+          gq[k] = c->Q[g[k]];
+          grank[k] = rank[g[k]];
+          gprim[k + 1] = gprim[k] + c->hpairs[g[k]].nprim;
+        }
+        for (int prec = 0; prec < (mixed ? 2 : 1); ++prec) {
+          std::vector<int> rbra, rbeg, rcnt;
+          long long q = 0, pq = 0;
+          for (int bi : bras) {
+            const double Qb = c->Q[bi];
+            // count of kets allowed by the canonical order (same class: rank <= rank(bra))
+            size_t n_order = g.size();
+            if (X == Y) n_order = std::upper_bound(grank.begin(), grank.end(), rank[bi]) - grank.begin();
+            // Schwarz: Q_b Q_k >= tau  (gq descending)
+            auto cnt_ge = [&](double thr) -> size_t {
+              if (thr <= 0.0) return g.size();
+              if (Qb <= 0.0) return 0;
+              const double need = thr / Qb;
+              size_t lo = 0, hi = g.size();
+              while (lo < hi) {
+                size_t mid = (lo + hi) / 2;
+                if ((double)gq[mid] >= need) lo = mid + 1; else hi = mid;
+              }
+              return lo;
+            };
+            size_t n_all = std::min(n_order, cnt_ge(tau));
+            size_t beg = 0, end = n_all;
+            if (mixed) {
+              size_t n64 = std::min(n_all, cnt_ge(tmix));
+              if (prec == 0) end = n64; else beg = n64;
+            }
+            if (end <= beg) continue;
+            rbra.push_back(bi);
+            rbeg.push_back((int)beg);
+            rcnt.push_back((int)(end - beg));
+            q += (long long)(end - beg);
+            pq += (long long)c->hpairs[bi].nprim * (gprim[end] - gprim[beg]);
+          }
+          if (rbra.empty()) continue;
+          Pending P{};
+          P.p.la = la; P.p.lb = lb; P.p.lc = lc; P.p.ld = ld;
+          P.p.prec = (mixed && prec == 1) ? PREC_FP32 : PREC_FP64;
+          P.p.quartets = q;
+          P.p.prim_quartets = pq;
+          P.bra = ints.size();
+          ints.insert(ints.end(), rbra.begin(), rbra.end());
+          P.ket = ints.size();
+          ints.insert(ints.end(), g.begin(), g.end());
+          P.beg = ints.size();
+          // row_beg indexes the shared ket list of this group
+          ints.insert(ints.end(), rbeg.begin(), rbeg.end());
+          P.cnt = ints.size();
+          ints.insert(ints.end(), rcnt.begin(), rcnt.end());
+          P.off = lls.size();
+          long long acc = 0;
+          for (int cnt : rcnt) { lls.push_back(acc); acc += (cnt + 31) / 32; }
+          lls.push_back(acc);
+          P.p.cl.nrows = (int)rbra.size();
+          P.p.cl.nwarps = acc;
+          pend.push_back(P);
+          const long long flops = pq * ((long long)vrr + setup_flops(L)) + q * ((long long)hrr + 12LL * neri);
+          if (P.p.prec == PREC_FP32) {
+            st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
+          } else {
+            st.shell_quartets_fp64 += q; st.prim_quartets_fp64 += pq; st.flops_fp64 += flops;
+          }
+        }
+      }
+    }
+  }
+  st.shell_quartets_screened = total_shell_quartets - st.shell_quartets_fp64 - st.shell_quartets_fp32;
+  CK(dalloc(&c->d_plan_int, ints.size()));
+  CK(dalloc(&c->d_plan_ll, lls.size()));
+  if (!ints.empty()) CK(cudaMemcpy(c->d_plan_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!lls.empty()) CK(cudaMemcpy(c->d_plan_ll, lls.data(), lls.size() * sizeof(long long), cudaMemcpyHostToDevice));
+  for (auto& P : pend) {
+    P.p.cl.bra_list = c->d_plan_int + P.bra;
+    P.p.cl.ket_list = c->d_plan_int + P.ket;
+    P.p.cl.row_beg = c->d_plan_int + P.beg;
+    P.p.cl.row_cnt = c->d_plan_int + P.cnt;
+    P.p.cl.row_warp_off = c->d_plan_ll + P.off;
+    c->plans.push_back(P.p);
+  }
+  st.launches_per_build = (int)c->plans.size() + 1;
+  if (!for_tensor) c->stats = st;
+  return FOCK_OK;
+}
+
+int compute_schwarz(fock_ctx* c) {
+  const int npairs = (int)c->hpairs.size();
+  std::vector<std::vector<int>> cls(kNumPairClasses);
+  for (int p = 0; p < npairs; ++p)
+    if (c->hpairs[p].nprim > 0) cls[c->hpairs[p].cls].push_back(p);
+  int* d_list = nullptr;
+  CK(dalloc(&d_list, npairs));
+  std::vector<int> all;
+  for (auto& v : cls) all.insert(all.end(), v.begin(), v.end());
+  CK(cudaMemcpy(d_list, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CK(cudaMemset(c->d_schwarz, 0, npairs * sizeof(float)));
+  EriArgs a = eri_args(c);
+  size_t off = 0;
+  for (int X = 0; X < kNumPairClasses; ++X) {
+    if (cls[X].empty()) continue;
+    int la = 0, lb = 0;
+    for (int x = 0; x <= kMaxL; ++x)
+      for (int y = 0; y <= x; ++y)
+        if (pair_class(x, y) == X) { la = x; lb = y; }
+    ClassLaunch cl{};
+    cl.bra_list = d_list + off;
+    cl.nrows = (int)cls[X].size();
+    cudaError_t e = launch_eri_class(la, lb, la, lb, cl, a, MODE_SCHWARZ, PREC_FP64, c->stream);
+    c->launches++;
+    if (e != cudaSuccess) { cudaFree(d_list); return map_cuda(e); }
+    off += cls[X].size();
+  }
+  c->Q.assign(npairs, 0.0f);
+  cudaError_t e = cudaMemcpyAsync(c->Q.data(), c->d_schwarz, npairs * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_list);
+  CK(e);
+  // the float Schwarz factor is rounded up so that screening stays conservative
+  for (auto& q : c->Q) q = std::nextafter(q, INFINITY);
+  return FOCK_OK;
+}
+
+int ensure_blas(fock_ctx* c) {
+  if (!c->blas) {
+    if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) return FOCK_ERR_CUDA;
+  }
+  if (!c->solver) {
+    if (cusolverDnCreate(&c->solver) != CUSOLVER_STATUS_SUCCESS) return FOCK_ERR_CUDA;
+  }
+  cublasSetStream(c->blas, c->stream);
+  cusolverDnSetStream(c->solver, c->stream);
+  return FOCK_OK;
+}
+
+void to_std(const fock_ctx* c, const double* in, double* out) {  // reference <-> textbook for n x n
+  const int n = c->nbf;
+  const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      out[(size_t)i * n + j] = flip ? in[(size_t)i * n + j] * c->fsign[i] * c->fsign[j] : in[(size_t)i * n + j];
+}
+
+}  // namespace
+
+namespace {
+// generated flop model (dispatch.cuh provides the per-class table)
+int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri) {
+  return fockgb::generated_class_flops(la, lb, lc, ld, hrr, neri);
+}
+}  // namespace
+
+extern "C" {
+
+void fock_options_default(fock_options* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->sign_convention = FOCK_SIGN_REFERENCE;
+  o->precision = FOCK_PREC_FP64;
+  o->eri_mode = FOCK_ERI_EXACT;
+  o->schwarz_eps = 1e-12;
+  o->mixed_threshold = 1e-4;
+  o->prim_eps = 1e-20;
+  o->group_by_contraction = 1;
+  o->max_iters = 100;
+  o->epsilon = 1e-6;
+  o->conv_mode = FOCK_CONV_COMMUTATOR;
+  o->guess = FOCK_GUESS_GWH;
+  o->diis_len = 16;
+  o->diis_start = 5;
+  o->energy_mode = 0;
+  o->final_fp64 = 1;
+  o->device = 0;
+}
+
+const char* fock_strerror(int code) {
+  switch (code) {
+    case FOCK_OK: return "ok";
+    case FOCK_ERR_INVALID_ARG: return "invalid argument";
+    case FOCK_ERR_UNSUPPORTED_L: return "unsupported angular momentum (l > 2)";
+    case FOCK_ERR_OOM: return "out of device memory";
+    case FOCK_ERR_TIMEOUT: return "device work timed out";
+    case FOCK_ERR_DIVERGED: return "SCF diverged (DIIS error not a normal number)";
+    case FOCK_ERR_NOT_CONVERGED: return "SCF did not converge";
+    case FOCK_ERR_CUDA: return "CUDA error";
+    case FOCK_ERR_TOO_LARGE: return "problem too large for this entry point";
+    case FOCK_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown error";
+  }
+}
+
+int fock_nbasis(const fock_ctx* c) { return c ? c->nbf : FOCK_ERR_INVALID_ARG; }
+long long fock_launch_count(const fock_ctx* c) { return c ? c->launches : 0; }
+
+int fock_get_stats(const fock_ctx* c, fock_stats* st) {
+  if (!c || !st) return FOCK_ERR_INVALID_ARG;
+  *st = c->stats;
+  return FOCK_OK;
+}
+
+int fock_set_stream(fock_ctx* c, void* stream) {
+  if (!c) return FOCK_ERR_INVALID_ARG;
+  c->stream = stream ? (cudaStream_t)stream : c->own_stream;
+  if (c->blas) cublasSetStream(c->blas, c->stream);
+  if (c->solver) cusolverDnSetStream(c->solver, c->stream);
+  return FOCK_OK;
+}
+
+void fock_ctx_destroy(fock_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->own_stream) cudaStreamSynchronize(c->own_stream);
+  dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
+  dfree(c->d_boys64); dfree(c->d_exp64); dfree(c->d_ref_lut); dfree(c->d_boys32);
+  dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
+  dfree(c->d_plan_int); dfree(c->d_plan_ll);
+  dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4);
+  dfree(c->d_tensor);
+  if (c->blas) cublasDestroy(c->blas);
+  if (c->solver) cusolverDnDestroy(c->solver);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
+}
+
+int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell, const fock_options* opt,
+                    fock_ctx** out) {
+  if (!out) return FOCK_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (!atoms || natom <= 0 || !shells || nshell <= 0) return FOCK_ERR_INVALID_ARG;
+  fock_options o;
+  if (opt) o = *opt; else fock_options_default(&o);
+  for (int s = 0; s < nshell; ++s) {
+    const fock_shell& sh = shells[s];
+    if (sh.l < 0 || sh.nprim <= 0 || sh.atom < 0 || sh.atom >= natom || !sh.exps || !sh.coefs) return FOCK_ERR_INVALID_ARG;
+    if (sh.l > kMaxL) return FOCK_ERR_UNSUPPORTED_L;
+    for (int k = 0; k < sh.nprim; ++k)
+      if (!(sh.exps[k] > 0.0) || !std::isfinite(sh.coefs[k])) return FOCK_ERR_INVALID_ARG;
+  }
+  for (int a = 0; a < natom; ++a)
+    if (!std::isfinite(atoms[a].x) || !std::isfinite(atoms[a].y) || !std::isfinite(atoms[a].z) || atoms[a].Z < 0)
+      return FOCK_ERR_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return FOCK_ERR_NO_DEVICE;
+  if (o.device < 0 || o.device >= ndev) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(o.device));
+  std::call_once(g_tab_once, build_tables);
+
+  fock_ctx* c = new fock_ctx();
+  c->opt = o;
+  c->device = o.device;
+  c->natom = natom;
+  c->atoms.assign(atoms, atoms + natom);
+  int f0 = 0;
+  for (int s = 0; s < nshell; ++s) {
+    const fock_shell& sh = shells[s];
+    HostShell h;
+    h.l = sh.l; h.atom = sh.atom; h.nprim = sh.nprim; h.f0 = f0;
+    h.c[0] = atoms[sh.atom].x; h.c[1] = atoms[sh.atom].y; h.c[2] = atoms[sh.atom].z;
+    for (int k = 0; k < sh.nprim; ++k) {
+      h.exps.push_back(sh.exps[k]);
+      h.coefs.push_back(sh.coefs[k] * prim_norm(sh.l, 0, 0, sh.exps[k]));
+    }
+    f0 += ncart(sh.l);
+    for (int k = 0; k < ncart(sh.l); ++k) c->fsign.push_back((sh.l & 1) ? -1.0 : 1.0);
+    c->shells.push_back(h);
+  }
+  c->nbf = f0;
+  int rc = FOCK_OK;
+  auto fail = [&](int code) { fock_ctx_destroy(c); return code; };
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FOCK_ERR_CUDA);
+  c->stream = c->own_stream;
+
+  // ---- shell pairs and primitive pairs ----
+  std::vector<PrimPair64> p64;
+  std::vector<PrimPair32> p32;
+  const double kpref = std::sqrt(2.0) * std::pow(M_PI, 1.25);
+  for (int i = 0; i < nshell; ++i)
+    for (int j = 0; j <= i; ++j) {
+      int a = i, b = j;
+      if (c->shells[j].l > c->shells[i].l) { a = j; b = i; }
+      const HostShell &A = c->shells[a], &B = c->shells[b];
+      PairInfo P{};
+      P.prim_off = (int)p64.size();
+      P.fa = A.f0; P.fb = B.f0; P.sa = a; P.sb = b;
+      P.cls = pair_class(A.l, B.l);
+      for (int k = 0; k < 3; ++k) P.AB[k] = A.c[k] - B.c[k];
+      const double ab2 = P.AB[0] * P.AB[0] + P.AB[1] * P.AB[1] + P.AB[2] * P.AB[2];
+      for (int pa = 0; pa < A.nprim; ++pa)
+        for (int pb = 0; pb < B.nprim; ++pb) {
+          const double ea = A.exps[pa], eb = B.exps[pb], p = ea + eb;
+          const double K = A.coefs[pa] * B.coefs[pb] * std::exp(-ea * eb / p * ab2) * kpref / p;
+          if (!(std::fabs(K) >= o.prim_eps)) continue;
+          double Pc[3], PA[3];
+          for (int k = 0; k < 3; ++k) {
+            Pc[k] = (ea * A.c[k] + eb * B.c[k]) / p;
+            PA[k] = Pc[k] - A.c[k];
+          }
+          PrimPair64 q;
+          q.v[0] = make_double2(p, 0.5 / p);
+          q.v[1] = make_double2(K, Pc[0]);
+          q.v[2] = make_double2(Pc[1], Pc[2]);
+          q.v[3] = make_double2(PA[0], PA[1]);
+          q.v[4] = make_double2(PA[2], 0.0);
+          p64.push_back(q);
+          PrimPair32 r;
+          r.v[0] = make_float4((float)p, (float)(0.5 / p), (float)K, (float)Pc[0]);
+          r.v[1] = make_float4((float)Pc[1], (float)Pc[2], (float)PA[0], (float)PA[1]);
+          r.v[2] = make_float4((float)PA[2], 0.f, 0.f, 0.f);
+          p32.push_back(r);
+        }
+      P.nprim = (int)p64.size() - P.prim_off;
+      c->hpairs.push_back(P);
+    }
+  c->nprim_pairs = (long long)p64.size();
+  const int npairs = (int)c->hpairs.size();
+  const size_t nn = (size_t)c->nbf * c->nbf;
+  if ((rc = map_cuda(dalloc(&c->d_pairs, npairs))) ||
+      (rc = map_cuda(dalloc(&c->d_prim64, p64.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_prim32, p32.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_boys64, g_boys64.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_boys32, g_boys32.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_exp64, g_exp64.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_ref_lut, g_ref_lut.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_schwarz, npairs))) ||
+      (rc = map_cuda(dalloc(&c->d_D, nn))) || (rc = map_cuda(dalloc(&c->d_M, nn))) ||
+      (rc = map_cuda(dalloc(&c->d_G, nn))) || (rc = map_cuda(dalloc(&c->d_D32, nn))))
+    return fail(rc);
+  if ((rc = map_cuda(cudaMemcpy(c->d_pairs, c->hpairs.data(), npairs * sizeof(PairInfo), cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_prim64, p64.data(), p64.size() * sizeof(PrimPair64), cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_prim32, p32.data(), p32.size() * sizeof(PrimPair32), cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_boys64, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_boys32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_exp64, g_exp64.data(), g_exp64.size() * 8, cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_ref_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice))))
+    return fail(rc);
+
+  // ---- per-function MD basis (one-electron integrals, reference-compatible tensor) ----
+  {
+    std::vector<MdFunc> fl;
+    std::vector<double> ex, cf;
+    for (const HostShell& h : c->shells) {
+      for (int x = 0; x <= h.l; ++x)
+        for (int y = 0; y <= h.l; ++y)
+          for (int z = 0; z <= h.l; ++z) {
+            if (x + y + z != h.l) continue;
+            MdFunc f;
+            f.c[0] = h.c[0]; f.c[1] = h.c[1]; f.c[2] = h.c[2];
+            f.ang[0] = x; f.ang[1] = y; f.ang[2] = z;
+            f.p0 = (int)ex.size();
+            f.np = h.nprim;
+            for (int k = 0; k < h.nprim; ++k) {
+              ex.push_back(h.exps[k]);
+              cf.push_back(shells[&h - &c->shells[0]].coefs[k] * prim_norm(x, y, z, h.exps[k]));
+            }
+            fl.push_back(f);
+          }
+    }
+    std::vector<double> at4;
+    for (int a = 0; a < natom; ++a) {
+      at4.push_back(atoms[a].x); at4.push_back(atoms[a].y); at4.push_back(atoms[a].z); at4.push_back((double)atoms[a].Z);
+    }
+    if ((rc = map_cuda(dalloc(&c->d_mdfuncs, fl.size()))) || (rc = map_cuda(dalloc(&c->d_mdexps, ex.size()))) ||
+        (rc = map_cuda(dalloc(&c->d_mdcoefs, cf.size()))) || (rc = map_cuda(dalloc(&c->d_atoms4, at4.size()))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_mdfuncs, fl.data(), fl.size() * sizeof(MdFunc), cudaMemcpyHostToDevice))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_mdexps, ex.data(), ex.size() * 8, cudaMemcpyHostToDevice))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_mdcoefs, cf.data(), cf.size() * 8, cudaMemcpyHostToDevice))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_atoms4, at4.data(), at4.size() * 8, cudaMemcpyHostToDevice))))
+      return fail(rc);
+  }
+
+  if ((rc = compute_schwarz(c)) != FOCK_OK) return fail(rc);
+  if ((rc = build_plan(c, false)) != FOCK_OK) return fail(rc);
+  *out = c;
+  return FOCK_OK;
+}
+
+int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
+  if (!c || (precision != FOCK_PREC_FP64 && precision != FOCK_PREC_MIXED) || !(mixed_threshold >= 0.0))
+    return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  c->opt.precision = precision;
+  c->opt.mixed_threshold = mixed_threshold;
+  return build_plan(c, false);
+}
+
+int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
+  if (!c || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
+  const int n = c->nbf;
+  const size_t nn = (size_t)n * n;
+  CK(cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), c->stream));
+  EriArgs a = eri_args(c);
+  a.D = D_dev;
+  bool need32 = false;
+  for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
+  if (need32) {
+    CK(k_to_float(D_dev, c->d_D32, (int)nn, c->stream));
+    c->launches++;
+  }
+  for (const Plan& p : c->plans) {
+    cudaError_t e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->stream);
+    c->launches++;
+    CK(e);
+  }
+  CK(k_symmetrize(c->d_M, G_dev, n, c->stream));
+  c->launches++;
+  return FOCK_OK;
+}
+
+int fock_build_jk(fock_ctx* c, const double* D, double* G) {
+  if (!c || !D || !G) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  const int n = c->nbf;
+  const size_t nn = (size_t)n * n;
+  std::vector<double> Ds(nn), Gs(nn);
+  to_std(c, D, Ds.data());
+  CK(cudaMemcpyAsync(c->d_D, Ds.data(), nn * 8, cudaMemcpyHostToDevice, c->stream));
+  int rc = fock_build_jk_device(c, c->d_D, c->d_G);
+  if (rc != FOCK_OK) return rc;
+  CK(cudaMemcpyAsync(Gs.data(), c->d_G, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  to_std(c, Gs.data(), G);
+  return FOCK_OK;
+}
+
+int fock_eri_tensor(fock_ctx* c, double* out) {
+  if (!c || !out) return FOCK_ERR_INVALID_ARG;
+  const size_t n = (size_t)c->nbf;
+  if (n > 160) return FOCK_ERR_TOO_LARGE;
+  CK(cudaSetDevice(c->device));
+  const size_t n4 = n * n * n * n;
+  double* d_t = nullptr;
+  CK(dalloc(&d_t, n4));
+  int rc = FOCK_OK;
+  cudaError_t e = cudaMemsetAsync(d_t, 0, n4 * 8, c->stream);
+  if (e == cudaSuccess) {
+    if (c->opt.eri_mode == FOCK_ERI_REFCOMPAT) {
+      double* d_diag = nullptr;
+      e = dalloc(&d_diag, n * (n + 1) / 2);
+      if (e == cudaSuccess) {
+        e = md_eri_tensor(md_basis(c), md_tables(c), MD_BOYS_LUT | MD_X_DEFECT, 1e-6, d_diag, d_t, c->stream);
+        c->launches += 2;
+        cudaStreamSynchronize(c->stream);
+        cudaFree(d_diag);
+      }
+    } else {
+      // all quartets, no screening: a temporary unscreened FP64 plan
+      fock_options keep = c->opt;
+      std::vector<Plan> keep_plans = c->plans;
+      int* keep_i = c->d_plan_int;
+      long long* keep_l = c->d_plan_ll;
+      c->d_plan_int = nullptr;
+      c->d_plan_ll = nullptr;
+      rc = build_plan(c, true);
+      if (rc == FOCK_OK) {
+        EriArgs a = eri_args(c);
+        a.tensor = d_t;
+        for (const Plan& p : c->plans) {
+          e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_TENSOR, PREC_FP64, c->stream);
+          c->launches++;
+          if (e != cudaSuccess) break;
+        }
+        cudaStreamSynchronize(c->stream);
+      }
+      dfree(c->d_plan_int);
+      dfree(c->d_plan_ll);
+      c->d_plan_int = keep_i;
+      c->d_plan_ll = keep_l;
+      c->plans = keep_plans;
+      c->opt = keep;
+    }
+  }
+  if (e == cudaSuccess && rc == FOCK_OK) e = cudaMemcpyAsync(out, d_t, n4 * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_t);
+  if (rc != FOCK_OK) return rc;
+  CK(e);
+  if (c->opt.sign_convention == FOCK_SIGN_REFERENCE) {
+    for (size_t l = 0; l < n; ++l)
+      for (size_t k = 0; k < n; ++k)
+        for (size_t j = 0; j < n; ++j) {
+          const double s = c->fsign[l] * c->fsign[k] * c->fsign[j];
+          double* row = out + ((l * n + k) * n + j) * n;
+          for (size_t i = 0; i < n; ++i) row[i] *= s * c->fsign[i];
+        }
+  }
+  return FOCK_OK;
+}
+
+int fock_one_electron(fock_ctx* c, double* S, double* T, double* V) {
+  if (!c || !S || !T || !V) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  const int n = c->nbf;
+  const size_t nn = (size_t)n * n;
+  double *dS = nullptr, *dT = nullptr, *dV = nullptr;
+  cudaError_t e = dalloc(&dS, nn);
+  if (e == cudaSuccess) e = dalloc(&dT, nn);
+  if (e == cudaSuccess) e = dalloc(&dV, nn);
+  const int flags = c->opt.eri_mode == FOCK_ERI_REFCOMPAT ? (MD_BOYS_LUT | MD_X_DEFECT) : 0;
+  if (e == cudaSuccess) {
+    e = md_one_electron(md_basis(c), md_tables(c), c->d_atoms4, c->natom, flags, dS, dT, dV, c->stream);
+    c->launches++;
+  }
+  std::vector<double> hS(nn), hT(nn), hV(nn);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hS.data(), dS, nn * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hT.data(), dT, nn * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hV.data(), dV, nn * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(dS); cudaFree(dT); cudaFree(dV);
+  CK(e);
+  to_std(c, hS.data(), S);
+  to_std(c, hT.data(), T);
+  to_std(c, hV.data(), V);
+  return FOCK_OK;
+}
+
+int fock_measure_fma_peak(int device, int fp64, double* gflops) {
+  if (!gflops) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, device));
+  const int threads = 256, blocks = prop.multiProcessorCount * 8;
+  const int iters = fp64 ? 2000 : 40000;
+  void* out = nullptr;
+  CK(cudaMalloc(&out, (size_t)blocks * threads * 8));
+  float ms = 0.f;
+  cudaError_t e = fma_peak(fp64, blocks, threads, iters, out, &ms);
+  cudaFree(out);
+  CK(e);
+  const double flops = 2.0 * 64.0 * (double)iters * blocks * threads;
+  *gflops = flops / (ms * 1e-3) / 1e9;
+  return FOCK_OK;
+}
+
+// ---------------------------------------------------------------------------
+// RHF (scf/src/lib.rs:73-258) on the device.  Column-major n x n buffers.
+// ---------------------------------------------------------------------------
+int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
+  if (!c || !res) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  auto t_start = std::chrono::steady_clock::now();
+  const int n = c->nbf;
+  const size_t nn = (size_t)n * n;
+  int ne = 0;
+  for (const fock_atom& a : c->atoms) ne += a.Z;
+  ne -= charge;
+  if (ne < 0 || ne > 2 * n) return FOCK_ERR_INVALID_ARG;
+  const int nocc = ne / 2;
+  double vnn = 0.0;
+  for (int i = 0; i < c->natom; ++i)
+    for (int j = i + 1; j < c->natom; ++j) {
+      const double dx = c->atoms[j].x - c->atoms[i].x, dy = c->atoms[j].y - c->atoms[i].y,
+                   dz = c->atoms[j].z - c->atoms[i].z;
+      vnn += (double)c->atoms[i].Z * c->atoms[j].Z / std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+  int rc = ensure_blas(c);
+  if (rc != FOCK_OK) return rc;
+  const bool refc = c->opt.eri_mode == FOCK_ERI_REFCOMPAT;
+  const int ring = std::max(1, std::min(c->opt.diis_len, 16));
+  // buffers
+  std::vector<double*> bufs;
+  auto mk = [&](size_t cnt) -> double* {
+    double* p = nullptr;
+    if (dalloc(&p, cnt) != cudaSuccess) return nullptr;
+    bufs.push_back(p);
+    return p;
+  };
+  double *S = mk(nn), *T = mk(nn), *V = mk(nn), *H = mk(nn), *X = mk(nn), *W = mk(nn), *U = mk(nn), *w = mk(n);
+  double *F = mk(nn), *Fd = mk(nn), *G = mk(nn), *Dm = mk(nn), *Dn = mk(nn), *C = mk(nn), *T1 = mk(nn), *T2 = mk(nn);
+  double *Fring = mk(nn * ring), *Ering = mk(nn * ring), *Bm = mk((size_t)ring * ring), *coef = mk(ring + 1);
+  double* scal = mk(4);  // [0] E_cur, [1] E_ref, [2] max|e| bits
+  int* d_order = nullptr;
+  int* d_info = nullptr;
+  cudaError_t e = dalloc(&d_order, ring);
+  if (e == cudaSuccess) e = dalloc(&d_info, 1);
+  bool ok = e == cudaSuccess;
+  for (double* p : bufs) ok = ok && p;
+  auto cleanup = [&]() {
+    for (double* p : bufs) cudaFree(p);
+    if (d_order) cudaFree(d_order);
+    if (d_info) cudaFree(d_info);
+  };
+  if (!ok) { cleanup(); return FOCK_ERR_OOM; }
+  cudaStream_t s = c->stream;
+  const double one = 1.0, zero = 0.0, two = 2.0;
+  int lwork = 0;
+  if (cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U, n, w, &lwork) !=
+      CUSOLVER_STATUS_SUCCESS) { cleanup(); return FOCK_ERR_CUDA; }
+  double* work = mk(lwork);
+  if (!work) { cleanup(); return FOCK_ERR_OOM; }
+  int fail = FOCK_OK;
+  auto cku = [&](cudaError_t x) { if (x != cudaSuccess && fail == FOCK_OK) fail = map_cuda(x); };
+  auto ckb = [&](cublasStatus_t x) { if (x != CUBLAS_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
+  auto cks = [&](cusolverStatus_t x) { if (x != CUSOLVER_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
+  auto gemm = [&](cublasOperation_t ta, cublasOperation_t tb, int k, const double* alpha, const double* A,
+                  const double* B, double* Cc) {
+    ckb(cublasDgemm(c->blas, ta, tb, n, n, k, alpha, A, n, B, n, &zero, Cc, n));
+    c->launches++;
+  };
+  // one-electron matrices (textbook convention internally)
+  const int flags = refc ? (MD_BOYS_LUT | MD_X_DEFECT) : 0;
+  cku(md_one_electron(md_basis(c), md_tables(c), c->d_atoms4, c->natom, flags, S, T, V, s));
+  cku(k_add(T, V, H, (int)nn, s));
+  c->launches += 2;
+  if (refc) {
+    if (n > 160) { cleanup(); return FOCK_ERR_TOO_LARGE; }
+    if (!c->d_tensor) {
+      const size_t n4 = nn * nn;
+      cku(dalloc(&c->d_tensor, n4));
+      double* d_diag = mk((size_t)n * (n + 1) / 2);
+      if (fail == FOCK_OK && d_diag) {
+        cku(cudaMemsetAsync(c->d_tensor, 0, n4 * 8, s));
+        cku(md_eri_tensor(md_basis(c), md_tables(c), MD_BOYS_LUT | MD_X_DEFECT, 1e-6, d_diag, c->d_tensor, s));
+        c->launches += 2;
+      }
+    }
+  }
+  // Loewdin X = U diag(w^-1/2) U^T (scf/src/lib.rs:139-146)
+  cku(cudaMemcpyAsync(U, S, nn * 8, cudaMemcpyDeviceToDevice, s));
+  cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U, n, w, work, lwork, d_info));
+  cku(k_scale_cols(U, w, W, n, s));
+  c->launches += 2;
+  gemm(CUBLAS_OP_N, CUBLAS_OP_T, n, &one, W, U, X);
+  std::vector<double> evals(n);
+  auto density_from = [&](const double* Fin, double* Dout) {
+    gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, &one, X, Fin, T1);  // X^T F
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, X, T2);   // X^T F X
+    cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, T2, n, w, work, lwork, d_info));
+    c->launches++;
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, X, T2, C);    // C = X C'
+    if (nocc > 0) {
+      ckb(cublasDgemm(c->blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &two, C, n, C, n, &zero, Dout, n));
+      c->launches++;
+    } else {
+      cku(cudaMemsetAsync(Dout, 0, nn * 8, s));
+    }
+  };
+  cku(k_guess(S, H, F, n, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, s));
+  c->launches++;
+  density_from(F, Dm);
+  if (fail != FOCK_OK) { cleanup(); return fail; }
+
+  std::vector<int> order;  // slots, oldest first
+  int next_slot = 0;
+  double e_prev = 0.0;
+  double fock_ms = 0.0;
+  int builds = 0;
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  int result = FOCK_ERR_DIVERGED;
+  const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
+  for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
+    cudaEventRecord(ev0, s);
+    if (refc) { cku(md_g_from_tensor(c->d_tensor, Dm, n, G, s)); c->launches++; }
+    else { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
+    cudaEventRecord(ev1, s);
+    builds++;
+    cku(k_add(H, G, F, (int)nn, s));
+    cku(cudaMemsetAsync(scal, 0, 4 * 8, s));
+    cku(k_energy(Dm, H, G, (int)nn, scal, s));            // consistent energy of Dm
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, F, Dm, T1);   // F D
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, S, T2);   // F D S
+    const int slot = next_slot;
+    next_slot = (next_slot + 1) % ring;
+    if ((int)order.size() == ring) order.erase(order.begin());
+    order.push_back(slot);
+    cku(k_commutator(T2, Ering + (size_t)slot * nn, n, (unsigned long long*)(scal + 2), s));
+    cku(cudaMemcpyAsync(Fring + (size_t)slot * nn, F, nn * 8, cudaMemcpyDeviceToDevice, s));
+    const int nused = (int)order.size();
+    cku(k_diis_dots(Ering, (int)nn, slot, std::max(nused, *std::max_element(order.begin(), order.end()) + 1), ring, Bm, s));
+    c->launches += 4;
+    const double* Fuse = F;
+    if (nused >= c->opt.diis_start) {
+      cku(cudaMemcpyAsync(d_order, order.data(), nused * sizeof(int), cudaMemcpyHostToDevice, s));
+      cku(k_diis_solve(Bm, ring, d_order, nused, coef, s));
+      cku(k_diis_extrapolate(Fring, (int)nn, d_order, nused, coef, slot, Fd, s));
+      c->launches += 2;
+      Fuse = Fd;
+    }
+    density_from(Fuse, Dn);
+    cku(k_energy(Dn, H, G, (int)nn, scal + 1, s));        // reference energy: new D, old G
+    c->launches++;
+    double hs[4];
+    cku(cudaMemcpyAsync(hs, scal, 4 * 8, cudaMemcpyDeviceToHost, s));
+    cku(cudaStreamSynchronize(s));
+    if (fail != FOCK_OK) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    fock_ms += ms;
+    unsigned long long bits;
+    std::memcpy(&bits, &hs[2], 8);
+    double err;
+    std::memcpy(&err, &bits, 8);
+    const double e_cur = hs[0], e_ref = hs[1];
+    bool done;
+    if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) done = err < c->opt.epsilon;
+    else done = iter > 0 && std::fabs(e_cur - e_prev) < c->opt.epsilon && err < std::sqrt(c->opt.epsilon);
+    if (done || iter == c->opt.max_iters) {
+      double e_report = c->opt.energy_mode == 0 ? e_ref : e_cur;
+      const double* Dfinal = c->opt.energy_mode == 0 ? Dn : Dm;
+      if (mixed && c->opt.final_fp64 && !refc) {
+        // refinement: one FP64 build on the converged density, consistent energy
+        fock_options keep = c->opt;
+        int r = fock_set_precision(c, FOCK_PREC_FP64, keep.mixed_threshold);
+        if (r == FOCK_OK) r = fock_build_jk_device(c, Dfinal, G);
+        builds++;
+        cku(cudaMemsetAsync(scal, 0, 8, s));
+        cku(k_energy(Dfinal, H, G, (int)nn, scal, s));
+        cku(cudaMemcpyAsync(hs, scal, 8, cudaMemcpyDeviceToHost, s));
+        cku(cudaStreamSynchronize(s));
+        fock_set_precision(c, FOCK_PREC_MIXED, keep.mixed_threshold);
+        if (r != FOCK_OK) { fail = r; break; }
+        e_report = hs[0];
+      }
+      res->electronic_energy = e_report;
+      res->total_energy = e_report + vnn;
+      res->nuclear_repulsion = vnn;
+      res->iterations = iter;
+      res->converged = done ? 1 : 0;
+      res->n_electrons = ne;
+      res->n_basis = n;
+      std::vector<double> hD(nn), hC(nn);
+      if (res->density_matrix || res->coefficient_matrix || res->orbital_energies) {
+        cku(cudaMemcpyAsync(hD.data(), Dfinal, nn * 8, cudaMemcpyDeviceToHost, s));
+        cku(cudaMemcpyAsync(hC.data(), C, nn * 8, cudaMemcpyDeviceToHost, s));
+        cku(cudaMemcpyAsync(evals.data(), w, n * 8, cudaMemcpyDeviceToHost, s));
+        cku(cudaStreamSynchronize(s));
+      }
+      const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
+      if (res->density_matrix)  // symmetric: column-major == row-major
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j)
+            res->density_matrix[(size_t)i * n + j] = hD[(size_t)j * n + i] * (flip ? c->fsign[i] * c->fsign[j] : 1.0);
+      if (res->coefficient_matrix)  // row-major C[i][k] (function i, orbital k)
+        for (int i = 0; i < n; ++i)
+          for (int k = 0; k < n; ++k)
+            res->coefficient_matrix[(size_t)i * n + k] = hC[(size_t)k * n + i] * (flip ? c->fsign[i] : 1.0);
+      if (res->orbital_energies) std::memcpy(res->orbital_energies, evals.data(), n * 8);
+      result = FOCK_OK;
+      break;
+    }
+    if (!std::isnormal(err)) { result = FOCK_ERR_DIVERGED; break; }
+    e_prev = e_cur;
+    std::swap(Dm, Dn);
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  res->fock_seconds = fock_ms * 1e-3;
+  res->fock_builds = builds;
+  res->scf_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  cleanup();
+  if (fail != FOCK_OK) return fail;
+  return result;
+}
+
+}  // extern "C"

@@ -1,0 +1,393 @@
+// McMurchie-Davidson integrals on the device, per basis function.
+//
+// These kernels follow the reference's own formulas function by function:
+//   hermite_expansion   basis/src/utils.rs:33-50   (Q = B - A)
+//   coulomb_auxiliary   basis/src/utils.rs:73-106  (C - P, P_cd - P_ab)
+//   _overlap/_kinetic/_nuclear_attraction/_electron_repulsion
+//                       basis/src/contracted_gaussian.rs:51-205
+// evaluated bottom-up in FP64.  They serve
+//   * the one-electron matrices S, T, V of the SCF (all modes), and
+//   * the dense ERI tensor of the reference-compatible mode
+//     (ElectronTensor::from_basis, electron_tensor.rs:81-176) including the
+//     reference Boys LUT, the x-branch recursion defect and the 1e-6
+//     function-level zeroing when the refcompat flags are set.
+// Results are converted to the textbook sign convention (factor (-1)^l per
+// function) before they are stored, so every internal matrix uses one
+// convention.  The hot path (fused ERI + J/K) lives in eri_kernel.cuh.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "md_device.cuh"
+
+namespace fockgb {
+
+// Reference Boys function (boys/src/lib.rs:58-81): F_10 tabulated at 0.15 k,
+// k < 200, linear interpolation (upper index clamped to 199), downward
+// recursion; asymptotic formula for t >= 30.
+__device__ double boys_ref_dev(double t, int n, const double* __restrict__ lut) {
+  if (fabs(t) < 1e-16) return 1.0 / (2 * n + 1);
+  if (fabs(t) >= 30.0) {
+    unsigned arg = (2u * (unsigned)n >= 1u) ? 2u * (unsigned)n - 1u : 0u;
+    unsigned df = 1;
+    for (unsigned k = 2 - arg % 2; arg > 0 && k <= arg; k += 2) df *= k;
+    double p2 = 1.0;
+    for (int i = 0; i < n + 1; ++i) p2 *= 2.0;
+    double tp = 1.0;
+    for (int i = 0; i < 2 * n + 1; ++i) tp *= t;
+    return (double)df * (1.0 / p2) * sqrt(M_PI * (1.0 / tp));
+  }
+  double index_f = 200.0 * t / 30.0;
+  double lower = floor(index_f), upper = ceil(index_f);
+  double int_t = index_f - lower;
+  int lo = (int)lower, up = (int)upper;
+  up = up < 199 ? up : 199;
+  double cur = int_t * lut[up] + (1.0 - int_t) * lut[lo];
+  double e = exp(-t);
+  for (int cn = 10; cn > n; --cn) cur = (2.0 * t * cur + e) / (double)(2 * cn - 1);
+  return cur;
+}
+
+// Accurate F_0..F_nmax by the Taylor table (see common.cuh), runtime order.
+__device__ void boys_exact_all(double T, int nmax, const double* __restrict__ tab,
+                               const double* __restrict__ etab, double* F) {
+  if (T < kBoysTmax) {
+    int i = __float2int_rn((float)T * 16.0f);
+    i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
+    const double d = T - (double)i * 0.0625;
+    const double* row = tab + ((size_t)nmax * kBoysPts + i) * kBoysTerms;
+    double f = row[kBoysTerms - 1];
+    for (int k = kBoysTerms - 2; k >= 0; --k) f = fma(f, d, row[k]);
+    F[nmax] = f;
+    if (nmax > 0) {
+      const double nd = -d;
+      double ex = fma(nd, 1.0 / 5040.0, 1.0 / 720.0);
+      ex = fma(ex, nd, 1.0 / 120.0);
+      ex = fma(ex, nd, 1.0 / 24.0);
+      ex = fma(ex, nd, 1.0 / 6.0);
+      ex = fma(ex, nd, 0.5);
+      ex = fma(ex, nd, 1.0);
+      ex = fma(ex, nd, 1.0);
+      ex *= etab[i];
+      for (int m = nmax; m > 0; --m) F[m - 1] = (2.0 * T * F[m] + ex) / (double)(2 * m - 1);
+    }
+  } else {
+    const double r = 1.0 / sqrt(T);
+    double f = 0.88622692545275801365 * r;
+    F[0] = f;
+    for (int m = 1; m <= nmax; ++m) {
+      f *= (double)(2 * m - 1) * 0.5 / T;
+      F[m] = f;
+    }
+  }
+}
+
+namespace {
+
+// E^{ij}_t for i <= LI, j <= LJ (hermite_expansion, utils.rs:33-50, Q = B - A).
+template <int LI, int LJ>
+struct ETable {
+  double e[LI + 1][LJ + 1][LI + LJ + 1];
+};
+
+template <int LI, int LJ>
+__device__ void etab_build(int li, int lj, double dist, double a, double b, ETable<LI, LJ>& E) {
+  const double p = a + b, q = a * b / p;
+  const double r2p = 1.0 / (2.0 * p), qa = q * dist / a, qb = q * dist / b;
+  for (int i = 0; i <= li; ++i)
+    for (int j = 0; j <= lj; ++j)
+      for (int t = 0; t <= i + j; ++t) {
+        double v;
+        if (i == 0 && j == 0) {
+          v = exp(-q * dist * dist);
+        } else if (j == 0) {
+          double em = t >= 1 ? E.e[i - 1][j][t - 1] : 0.0;
+          double e0 = t <= i - 1 + j ? E.e[i - 1][j][t] : 0.0;
+          double ep = t + 1 <= i - 1 + j ? E.e[i - 1][j][t + 1] : 0.0;
+          v = r2p * em - qa * e0 + (double)(t + 1) * ep;
+        } else {
+          double em = t >= 1 ? E.e[i][j - 1][t - 1] : 0.0;
+          double e0 = t <= i + j - 1 ? E.e[i][j - 1][t] : 0.0;
+          double ep = t + 1 <= i + j - 1 ? E.e[i][j - 1][t + 1] : 0.0;
+          v = r2p * em + qb * e0 + (double)(t + 1) * ep;
+        }
+        E.e[i][j][t] = v;
+      }
+}
+
+// Compact index of (t, u, v), t + u + v = s: triples of smaller sum first,
+// then t ascending, then u ascending.
+__device__ __forceinline__ int cidx(int t, int u, int v) {
+  const int s = t + u + v;
+  return s * (s + 1) * (s + 2) / 6 + t * (s + 1) - t * (t - 1) / 2 + u;
+}
+
+// R^0_{tuv}, t+u+v <= L <= LMAX (coulomb_auxiliary, utils.rs:73-106); x_defect
+// keeps the reference's weight 1 on R_{t-2} in the x branch.
+template <int LMAX>
+struct RTable {
+  static constexpr int kN = (LMAX + 1) * (LMAX + 2) * (LMAX + 3) / 6;
+  double r[kN];
+  __device__ __forceinline__ double at(int t, int u, int v) const { return r[cidx(t, u, v)]; }
+};
+
+template <int LMAX>
+__device__ void rtab_build(int L, double p, const double d[3], double r2, int flags, const MdTables& tb,
+                           RTable<LMAX>& out) {
+  double F[LMAX + 1];
+  const double T = p * r2;
+  if (flags & MD_BOYS_LUT) {
+    for (int n = 0; n <= L; ++n) F[n] = boys_ref_dev(T, n, tb.ref_lut);
+  } else {
+    boys_exact_all(T, L, tb.boys64, tb.exp64, F);
+  }
+  RTable<LMAX> nxt;
+  for (int n = L; n >= 0; --n) {
+    const int lmax = L - n;
+    double pw = 1.0;
+    for (int k = 0; k < n; ++k) pw *= -2.0 * p;
+    for (int t = 0; t <= lmax; ++t)
+      for (int u = 0; u + t <= lmax; ++u)
+        for (int v = 0; v + u + t <= lmax; ++v) {
+          double val;
+          if (t == 0 && u == 0 && v == 0) val = pw * F[n];
+          else if (t == 0 && u == 0) val = d[2] * nxt.at(t, u, v - 1) + (v > 1 ? (double)(v - 1) * nxt.at(t, u, v - 2) : 0.0);
+          else if (t == 0) val = d[1] * nxt.at(t, u - 1, v) + (u > 1 ? (double)(u - 1) * nxt.at(t, u - 2, v) : 0.0);
+          else {
+            double fac = (flags & MD_X_DEFECT) ? 1.0 : (double)(t - 1);
+            val = d[0] * nxt.at(t - 1, u, v) + (t > 1 ? fac * nxt.at(t - 2, u, v) : 0.0);
+          }
+          out.r[cidx(t, u, v)] = val;
+        }
+    if (n > 0)
+      for (int k = 0; k < RTable<LMAX>::kN; ++k) nxt.r[k] = out.r[k];
+  }
+}
+
+__device__ __forceinline__ double fsign(const MdFunc& f) {
+  return ((f.ang[0] + f.ang[1] + f.ang[2]) & 1) ? -1.0 : 1.0;
+}
+
+__device__ double prim_overlap(const int A[3], double a, const int B[3], double b, const double diff[3]) {
+  for (int k = 0; k < 3; ++k)
+    if (A[k] < 0 || B[k] < 0) return 0.0;
+  double s = 1.0;
+  for (int k = 0; k < 3; ++k) {
+    ETable<2, 4> E;
+    etab_build(A[k], B[k], diff[k], a, b, E);
+    s *= E.e[A[k]][B[k]][0];
+  }
+  const double pp = M_PI / (a + b);
+  return s * sqrt(pp * pp * pp);
+}
+
+__device__ double prim_kinetic(const int A[3], double a, const int B[3], double b, const double diff[3]) {
+  const int l2 = B[0], m2 = B[1], n2 = B[2];
+  int Bs[3];
+  auto step = [&](int i, int j, int k) {
+    Bs[0] = B[0] + i; Bs[1] = B[1] + j; Bs[2] = B[2] + k;
+    return prim_overlap(A, a, Bs, b, diff);
+  };
+  const double term0 = b * (double)(2 * (l2 + m2 + n2) + 3) * prim_overlap(A, a, B, b, diff);
+  const double term1 = -2.0 * b * b * (step(2, 0, 0) + step(0, 2, 0) + step(0, 0, 2));
+  const double term2 = -0.5 * ((double)(l2 * (l2 - 1)) * step(-2, 0, 0) + (double)(m2 * (m2 - 1)) * step(0, -2, 0) +
+                               (double)(n2 * (n2 - 1)) * step(0, 0, -2));
+  return term0 + term1 + term2;
+}
+
+}  // namespace
+
+// S, T, V for function pairs i <= j; one thread per pair.
+__global__ void one_electron_kernel(const MdBasis B, const MdTables tb, const double* __restrict__ atoms /*x,y,z,Z*/,
+                                    int natom, int flags, double* S, double* T, double* V) {
+  const int n = B.nfunc;
+  const long long npair = (long long)n * (n + 1) / 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= npair) return;
+  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+  while ((long long)i * (i + 1) / 2 > t) --i;
+  const int j = (int)(t - (long long)i * (i + 1) / 2);
+  const MdFunc fa = B.funcs[j], fb = B.funcs[i];  // j <= i
+  const double diff[3] = {fb.c[0] - fa.c[0], fb.c[1] - fa.c[1], fb.c[2] - fa.c[2]};
+  double s = 0.0, k = 0.0, v = 0.0;
+  for (int pa = 0; pa < fa.np; ++pa)
+    for (int pb = 0; pb < fb.np; ++pb) {
+      const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
+      const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb];
+      s += cc * prim_overlap(fa.ang, a, fb.ang, b, diff);
+      k += cc * prim_kinetic(fa.ang, a, fb.ang, b, diff);
+      // nuclear attraction: -Z 2pi/p sum E E E R(p, C - P)
+      const double p = a + b;
+      double P[3];
+      for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / p;
+      ETable<2, 2> E[3];
+      for (int x = 0; x < 3; ++x) etab_build(fa.ang[x], fb.ang[x], diff[x], a, b, E[x]);
+      const int L = fa.ang[0] + fa.ang[1] + fa.ang[2] + fb.ang[0] + fb.ang[1] + fb.ang[2];
+      for (int c = 0; c < natom; ++c) {
+        const double dcp[3] = {atoms[4 * c] - P[0], atoms[4 * c + 1] - P[1], atoms[4 * c + 2] - P[2]};
+        const double r2 = dcp[0] * dcp[0] + dcp[1] * dcp[1] + dcp[2] * dcp[2];
+        RTable<4> R;
+        rtab_build(L, p, dcp, r2, flags, tb, R);
+        double sum = 0.0;
+        for (int tt = 0; tt <= fa.ang[0] + fb.ang[0]; ++tt)
+          for (int u = 0; u <= fa.ang[1] + fb.ang[1]; ++u)
+            for (int w = 0; w <= fa.ang[2] + fb.ang[2]; ++w)
+              sum += E[0].e[fa.ang[0]][fb.ang[0]][tt] * E[1].e[fa.ang[1]][fb.ang[1]][u] *
+                     E[2].e[fa.ang[2]][fb.ang[2]][w] * R.at(tt, u, w);
+        v += cc * (-atoms[4 * c + 3] * (2.0 * M_PI) / p * sum);
+      }
+    }
+  const double sg = fsign(fa) * fsign(fb);  // reference -> textbook convention
+  s *= sg; k *= sg; v *= sg;
+  S[(size_t)i * n + j] = s; S[(size_t)j * n + i] = s;
+  T[(size_t)i * n + j] = k; T[(size_t)j * n + i] = k;
+  V[(size_t)i * n + j] = v; V[(size_t)j * n + i] = v;
+}
+
+__device__ double md_eri_contracted(const MdBasis& B, const MdTables& tb, int ia, int ib, int ic, int id, int flags) {
+  const MdFunc fa = B.funcs[ia], fb = B.funcs[ib], fc = B.funcs[ic], fd = B.funcs[id];
+  double dab[3], dcd[3];
+  for (int k = 0; k < 3; ++k) { dab[k] = fb.c[k] - fa.c[k]; dcd[k] = fd.c[k] - fc.c[k]; }
+  const int L = fa.ang[0] + fa.ang[1] + fa.ang[2] + fb.ang[0] + fb.ang[1] + fb.ang[2] + fc.ang[0] + fc.ang[1] +
+                fc.ang[2] + fd.ang[0] + fd.ang[1] + fd.ang[2];
+  double sum = 0.0;
+  for (int pa = 0; pa < fa.np; ++pa)
+    for (int pb = 0; pb < fb.np; ++pb) {
+      const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
+      double Pab[3];
+      for (int k = 0; k < 3; ++k) Pab[k] = (a * fa.c[k] + b * fb.c[k]) / (a + b);
+      ETable<2, 2> Eab[3];
+      for (int k = 0; k < 3; ++k) etab_build(fa.ang[k], fb.ang[k], dab[k], a, b, Eab[k]);
+      const double cab = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb];
+      for (int pc = 0; pc < fc.np; ++pc)
+        for (int pd = 0; pd < fd.np; ++pd) {
+          const double c = B.exps[fc.p0 + pc], d = B.exps[fd.p0 + pd];
+          double cdiff[3];
+          for (int k = 0; k < 3; ++k) cdiff[k] = (c * fc.c[k] + d * fd.c[k]) / (c + d) - Pab[k];
+          const double r2 = cdiff[0] * cdiff[0] + cdiff[1] * cdiff[1] + cdiff[2] * cdiff[2];
+          ETable<2, 2> Ecd[3];
+          for (int k = 0; k < 3; ++k) etab_build(fc.ang[k], fd.ang[k], dcd[k], c, d, Ecd[k]);
+          const double p = a + b, q = c + d, alpha = p * q / (p + q);
+          RTable<8> R;
+          rtab_build(L, alpha, cdiff, r2, flags, tb, R);
+          double s = 0.0;
+          for (int t1 = 0; t1 <= fa.ang[0] + fb.ang[0]; ++t1)
+            for (int u1 = 0; u1 <= fa.ang[1] + fb.ang[1]; ++u1)
+              for (int v1 = 0; v1 <= fa.ang[2] + fb.ang[2]; ++v1) {
+                const double e123 = Eab[0].e[fa.ang[0]][fb.ang[0]][t1] * Eab[1].e[fa.ang[1]][fb.ang[1]][u1] *
+                                    Eab[2].e[fa.ang[2]][fb.ang[2]][v1];
+                for (int t2 = 0; t2 <= fc.ang[0] + fd.ang[0]; ++t2)
+                  for (int u2 = 0; u2 <= fc.ang[1] + fd.ang[1]; ++u2)
+                    for (int v2 = 0; v2 <= fc.ang[2] + fd.ang[2]; ++v2) {
+                      const double e456 = Ecd[0].e[fc.ang[0]][fd.ang[0]][t2] * Ecd[1].e[fc.ang[1]][fd.ang[1]][u2] *
+                                          Ecd[2].e[fc.ang[2]][fd.ang[2]][v2];
+                      s += e123 * e456 * R.at(t1 + t2, u1 + u2, v1 + v2) * (((t2 + u2 + v2) & 1) ? -1.0 : 1.0);
+                    }
+              }
+          const double pref = 2.0 * sqrt(M_PI * M_PI * M_PI * M_PI * M_PI) / (p * q * sqrt(p + q));
+          sum += cab * B.coefs[fc.p0 + pc] * B.coefs[fd.p0 + pd] * pref * s;
+        }
+    }
+  return sum * fsign(fa) * fsign(fb) * fsign(fc) * fsign(fd);
+}
+
+__device__ __forceinline__ void pair_of(long long P, int& i, int& j) {
+  int x = (int)((sqrt(8.0 * (double)P + 1.0) - 1.0) * 0.5);
+  while ((long long)(x + 1) * (x + 2) / 2 <= P) ++x;
+  while ((long long)x * (x + 1) / 2 > P) --x;
+  i = x;
+  j = (int)(P - (long long)x * (x + 1) / 2);
+}
+
+// (ij|ij) for every function pair P = i(i+1)/2 + j.
+__global__ void md_diag_kernel(const MdBasis B, const MdTables tb, int flags, double* diag) {
+  const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
+  const long long P = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (P >= np) return;
+  int i, j;
+  pair_of(P, i, j);
+  diag[P] = md_eri_contracted(B, tb, i, j, i, j, flags);
+}
+
+// Canonical quartets q in [q0, q0 + count): q = P(P+1)/2 + Q, P >= Q pair
+// indices.  Writes all eight images of (ij|kl) into the full tensor.
+// screen > 0: zero when sqrt((ij|ij)(kl|kl)) <= screen (electron_tensor.rs:134-155).
+__global__ void md_tensor_kernel(const MdBasis B, const MdTables tb, int flags, double screen,
+                                 const double* __restrict__ diag, long long q0, long long count, double* out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= count) return;
+  const long long q = q0 + t;
+  int Pi, Pj;
+  pair_of(q, Pi, Pj);  // Pi >= Pj as pair indices
+  const long long P = Pi, Q = Pj;
+  int i, j, k, l;
+  pair_of(P, i, j);
+  pair_of(Q, k, l);
+  double v;
+  if (P == Q) {
+    v = diag[P];
+  } else if (screen > 0.0 && !(sqrt(diag[P] * diag[Q]) > screen)) {
+    v = 0.0;
+  } else {
+    v = md_eri_contracted(B, tb, i, j, k, l, flags);
+  }
+  const size_t n = (size_t)B.nfunc;
+  const size_t I = i, J = j, K = k, Lq = l;
+  out[((Lq * n + K) * n + J) * n + I] = v;
+  out[((Lq * n + K) * n + I) * n + J] = v;
+  out[((K * n + Lq) * n + J) * n + I] = v;
+  out[((K * n + Lq) * n + I) * n + J] = v;
+  out[((J * n + I) * n + Lq) * n + K] = v;
+  out[((J * n + I) * n + K) * n + Lq] = v;
+  out[((I * n + J) * n + Lq) * n + K] = v;
+  out[((I * n + J) * n + K) * n + Lq] = v;
+}
+
+// G = J - K/2 from the full tensor, as scf/src/lib.rs:167-187:
+// G_ij = sum_xy D_xy ((ij|xy) - 1/2 (ix|jy)).  One thread per (i, j).
+__global__ void g_from_tensor_kernel(const double* __restrict__ eri, const double* __restrict__ D, int n, double* G) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int i = t / n, j = t % n;
+  const size_t N = (size_t)n;
+  double acc = 0.0;
+  for (int y = 0; y < n; ++y)
+    for (int x = 0; x < n; ++x)
+      acc += D[(size_t)x * n + y] * (eri[((y * N + x) * N + j) * N + i] - 0.5 * eri[((y * N + j) * N + x) * N + i]);
+  G[(size_t)i * n + j] = acc;
+}
+
+cudaError_t md_one_electron(const MdBasis& B, const MdTables& tb, const double* atoms, int natom, int flags,
+                            double* S, double* T, double* V, cudaStream_t s) {
+  const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
+  const int thr = 64;
+  one_electron_kernel<<<(unsigned)((np + thr - 1) / thr), thr, 0, s>>>(B, tb, atoms, natom, flags, S, T, V);
+  return cudaGetLastError();
+}
+
+cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, double screen, double* diag, double* out,
+                          cudaStream_t s) {
+  const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
+  const long long nq = np * (np + 1) / 2;
+  const int thr = 64;
+  md_diag_kernel<<<(unsigned)((np + thr - 1) / thr), thr, 0, s>>>(B, tb, flags, diag);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long long chunk = 1LL << 22;
+  for (long long q0 = 0; q0 < nq; q0 += chunk) {
+    const long long cnt = (nq - q0) < chunk ? (nq - q0) : chunk;
+    md_tensor_kernel<<<(unsigned)((cnt + thr - 1) / thr), thr, 0, s>>>(B, tb, flags, screen, diag, q0, cnt, out);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* G, cudaStream_t s) {
+  const int thr = 128;
+  g_from_tensor_kernel<<<(n * n + thr - 1) / thr, thr, 0, s>>>(eri, D, n, G);
+  return cudaGetLastError();
+}
+
+}  // namespace fockgb

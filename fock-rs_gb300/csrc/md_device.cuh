@@ -1,0 +1,38 @@
+// Per-function McMurchie-Davidson integrals (one-electron matrices, the
+// reference-compatible dense ERI tensor).  See md_device.cu.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace fockgb {
+
+enum MdFlags {
+  MD_BOYS_LUT = 1,   // reference Boys function (boys/src/lib.rs:58-81)
+  MD_X_DEFECT = 2,   // reference x-branch weight in coulomb_auxiliary (utils.rs:98-104)
+};
+
+struct MdFunc {
+  double c[3];  // centre, bohr
+  int ang[3];   // Cartesian exponents
+  int p0, np;   // primitive range
+};
+
+struct MdBasis {
+  const MdFunc* funcs;
+  const double* exps;
+  const double* coefs;  // normalised per Cartesian component (primitives.rs:19-27)
+  int nfunc;
+};
+
+struct MdTables {
+  const double* boys64;   // Taylor table (common.cuh)
+  const double* exp64;
+  const double* ref_lut;  // 200 values F_10(0.15 k)
+};
+
+cudaError_t md_one_electron(const MdBasis& B, const MdTables& tb, const double* atoms, int natom, int flags,
+                            double* S, double* T, double* V, cudaStream_t s);
+cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, double screen, double* diag, double* out,
+                          cudaStream_t s);
+cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* G, cudaStream_t s);
+
+}  // namespace fockgb

@@ -1,0 +1,236 @@
+// Small device kernels of the RHF loop (all FP64, column-major n x n, the
+// matrices involved are symmetric unless stated): Fock assembly, energy and
+// DIIS error reductions, the Pulay DIIS solve and extrapolation, guesses.
+// The dense products and the eigensolver are cuBLAS / cuSOLVER calls made
+// from fock_api.cu.
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "scf_device.cuh"
+
+namespace fockgb {
+
+__global__ void add_kernel(const double* a, const double* b, double* c, int nn) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nn) c[t] = a[t] + b[t];
+}
+
+// G = M + M^T (row-major M); optional output sign s_i s_j.
+__global__ void symmetrize_kernel(const double* M, double* G, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int i = t / n, j = t % n;
+  G[t] = M[(size_t)i * n + j] + M[(size_t)j * n + i];
+}
+
+__global__ void to_float_kernel(const double* a, float* b, int nn) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nn) b[t] = (float)a[t];
+}
+
+// GWH guess 0.875 S_ij (H_ii + H_jj) (scf/src/lib.rs:150-162) or F = H.
+__global__ void guess_kernel(const double* S, const double* H, double* F, int n, int gwh) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int i = t % n, j = t / n;
+  F[t] = gwh ? 0.875 * S[t] * (H[(size_t)i * n + i] + H[(size_t)j * n + j]) : H[t];
+}
+
+// X = U diag(w^{-1/2}) U^T  step 1: W = U diag(w^{-1/2}) (column scaling)
+__global__ void scale_cols_kernel(const double* U, const double* w, double* W, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * n) return;
+  const int col = t / n;
+  W[t] = U[t] / sqrt(w[col]);
+}
+
+// out[0] += 0.5 * sum D (2H + G)
+__global__ void energy_kernel(const double* D, const double* H, const double* G, int nn, double* out) {
+  double acc = 0.0;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nn; t += gridDim.x * blockDim.x)
+    acc += 0.5 * D[t] * (2.0 * H[t] + G[t]);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = acc;
+  __syncthreads();
+  if (w == 0) {
+    acc = lane < (blockDim.x >> 5) ? sm[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) atomicAdd(out, acc);
+  }
+}
+
+// E = A - A^T (A = F D S column-major) and out[0] = max |E| (as a non-negative
+// double, compared through its bit pattern).
+__global__ void commutator_kernel(const double* A, double* E, int n, unsigned long long* maxbits) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (t < n * n) {
+    const int r = t % n, c = t / n;
+    v = A[t] - A[(size_t)r * n + c];
+    E[t] = v;
+  }
+  double a = fabs(v);
+  if (isnan(v)) a = INFINITY;
+  for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(a));
+}
+
+// B[slot][k] = B[k][slot] = <E_slot, E_k> for the k in use; one block per k.
+__global__ void diis_dots_kernel(const double* Ering, int nn, int slot, int used_mask_n, int ring, double* B) {
+  const int k = blockIdx.x;
+  if (k >= used_mask_n) return;
+  const double* a = Ering + (size_t)slot * nn;
+  const double* b = Ering + (size_t)k * nn;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < nn; t += blockDim.x) acc += a[t] * b[t];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sm[i];
+    B[slot * ring + k] = s;
+    B[k * ring + slot] = s;
+  }
+}
+
+// Pulay DIIS: solve [B -1; -1 0] c = [0; -1] over the m slots listed in
+// order[0..m) (oldest first) by Gaussian elimination with partial pivoting
+// (the reference inverts the same matrix, scf/src/utils.rs:102-138).
+// coef[0..m) receives c; coef[m] = 1 on success, 0 if singular.
+__global__ void diis_solve_kernel(const double* B, int ring, const int* order, int m, double* coef) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double A[17 * 17], rhs[17];
+  const int M = m + 1;
+  for (int i = 0; i < m; ++i) {
+    for (int j = 0; j < m; ++j) A[i * M + j] = B[order[i] * ring + order[j]];
+    A[i * M + m] = -1.0;
+    A[m * M + i] = -1.0;
+    rhs[i] = 0.0;
+  }
+  A[m * M + m] = 0.0;
+  rhs[m] = -1.0;
+  bool ok = true;
+  for (int c = 0; c < M && ok; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < M; ++r)
+      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
+    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
+    if (piv != c) {
+      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
+      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
+    }
+    for (int r = c + 1; r < M; ++r) {
+      const double f = A[r * M + c] / A[c * M + c];
+      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
+      rhs[r] -= f * rhs[c];
+    }
+  }
+  if (ok) {
+    for (int c = M - 1; c >= 0; --c) {
+      double s = rhs[c];
+      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
+      rhs[c] = s / A[c * M + c];
+      if (!isfinite(rhs[c])) ok = false;
+    }
+  }
+  for (int i = 0; i < m; ++i) coef[i] = ok ? rhs[i] : 0.0;
+  coef[m] = ok ? 1.0 : 0.0;
+}
+
+// Fd = sum_i c_i F_{order[i]}; falls back to F_{last} when the solve failed.
+__global__ void diis_extrapolate_kernel(const double* Fring, int nn, const int* order, int m, const double* coef,
+                                        int last, double* Fd) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn) return;
+  if (coef[m] == 0.0) { Fd[t] = Fring[(size_t)last * nn + t]; return; }
+  double acc = 0.0;
+  for (int i = 0; i < m; ++i) acc += coef[i] * Fring[(size_t)order[i] * nn + t];
+  Fd[t] = acc;
+}
+
+// FP64 / FP32 FMA throughput probe: 8 independent chains per thread.
+template <typename T>
+__global__ void fma_peak_kernel(T* out, int iters, T b, T c) {
+  T a0 = (T)threadIdx.x * (T)1e-6, a1 = a0 + (T)1, a2 = a0 + (T)2, a3 = a0 + (T)3;
+  T a4 = a0 + (T)4, a5 = a0 + (T)5, a6 = a0 + (T)6, a7 = a0 + (T)7;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+      a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+}
+
+static unsigned blocks_for(long long n, int thr) { return (unsigned)((n + thr - 1) / thr); }
+
+cudaError_t k_add(const double* a, const double* b, double* c, int nn, cudaStream_t s) {
+  add_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, c, nn);
+  return cudaGetLastError();
+}
+cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s) {
+  symmetrize_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(M, G, n);
+  return cudaGetLastError();
+}
+cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s) {
+  to_float_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, nn);
+  return cudaGetLastError();
+}
+cudaError_t k_guess(const double* S, const double* H, double* F, int n, int gwh, cudaStream_t s) {
+  guess_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(S, H, F, n, gwh);
+  return cudaGetLastError();
+}
+cudaError_t k_scale_cols(const double* U, const double* w, double* W, int n, cudaStream_t s) {
+  scale_cols_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(U, w, W, n);
+  return cudaGetLastError();
+}
+cudaError_t k_energy(const double* D, const double* H, const double* G, int nn, double* out, cudaStream_t s) {
+  int blocks = (int)blocks_for(nn, 256);
+  if (blocks > 128) blocks = 128;
+  energy_kernel<<<blocks, 256, 0, s>>>(D, H, G, nn, out);
+  return cudaGetLastError();
+}
+cudaError_t k_commutator(const double* A, double* E, int n, unsigned long long* maxbits, cudaStream_t s) {
+  commutator_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(A, E, n, maxbits);
+  return cudaGetLastError();
+}
+cudaError_t k_diis_dots(const double* Ering, int nn, int slot, int nused, int ring, double* B, cudaStream_t s) {
+  diis_dots_kernel<<<nused, 256, 0, s>>>(Ering, nn, slot, nused, ring, B);
+  return cudaGetLastError();
+}
+cudaError_t k_diis_solve(const double* B, int ring, const int* order, int m, double* coef, cudaStream_t s) {
+  diis_solve_kernel<<<1, 32, 0, s>>>(B, ring, order, m, coef);
+  return cudaGetLastError();
+}
+cudaError_t k_diis_extrapolate(const double* Fring, int nn, const int* order, int m, const double* coef, int last,
+                               double* Fd, cudaStream_t s) {
+  diis_extrapolate_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(Fring, nn, order, m, coef, last, Fd);
+  return cudaGetLastError();
+}
+
+cudaError_t fma_peak(int fp64, int blocks, int threads, int iters, void* out, float* ms) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  // warm-up
+  if (fp64) fma_peak_kernel<double><<<blocks, threads>>>((double*)out, iters / 10 + 1, 0.999999, 1e-7);
+  else fma_peak_kernel<float><<<blocks, threads>>>((float*)out, iters / 10 + 1, 0.9999f, 1e-4f);
+  cudaEventRecord(e0);
+  if (fp64) fma_peak_kernel<double><<<blocks, threads>>>((double*)out, iters, 0.999999, 1e-7);
+  else fma_peak_kernel<float><<<blocks, threads>>>((float*)out, iters, 0.9999f, 1e-4f);
+  cudaEventRecord(e1);
+  cudaError_t e = cudaEventSynchronize(e1);
+  cudaEventElapsedTime(ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+}  // namespace fockgb

@@ -1,0 +1,184 @@
+/*
+ * fock_gb300.h -- C ABI of the GB300 (sm_103a) ERI + Fock-build library.
+ *
+ * Drop-in boundary for the Hartree-Fock hot path of fock-rs:
+ *   - the electron-repulsion tensor   ElectronTensor::from_basis
+ *       (basis/src/electron_tensor.rs:81) and its Index<(usize,usize,usize,usize)>
+ *       (basis/src/electron_tensor.rs:179-187)
+ *   - the Fock two-electron build     scf/src/lib.rs:167-187 (G = J - K/2)
+ *   - the RHF driver                  SelfConsistentField::try_scf
+ *       (scf/src/lib.rs:61-66, 73-258) -> HartreeFockResult (scf/src/lib.rs:27-37)
+ *   - the per-function integral       BasisFunction::electron_repulsion_int
+ *       (basis/src/lib.rs:41) through fock_eri_tensor on small bases
+ *
+ * Plain C: caller-owned host arrays, opaque context, int status codes (0 = ok,
+ * < 0 = error, fock_strerror for text).  Nothing aborts.  All matrices are
+ * row-major n_basis x n_basis doubles, basis functions in the reference's
+ * order: shells in input order, Cartesian components x-outer/z-inner
+ * ascending (p = z,y,x; d = zz,yz,yy,xz,xy,xx, basis_set/src/lib.rs:88-100).
+ *
+ * Threading: one context per host thread; calls on one context run in order
+ * on its CUDA stream and return after the result is on the host.
+ */
+#ifndef FOCK_GB300_H
+#define FOCK_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define FOCK_OK 0
+#define FOCK_ERR_INVALID_ARG (-1)
+#define FOCK_ERR_UNSUPPORTED_L (-2)
+#define FOCK_ERR_OOM (-3)
+#define FOCK_ERR_TIMEOUT (-4)
+#define FOCK_ERR_DIVERGED (-5)
+#define FOCK_ERR_NOT_CONVERGED (-6)
+#define FOCK_ERR_CUDA (-7)
+#define FOCK_ERR_TOO_LARGE (-8)
+#define FOCK_ERR_NO_DEVICE (-9)
+
+/* ---- option values ---- */
+#define FOCK_SIGN_REFERENCE 0 /* phi ~ (A - r)^l, as contracted_gaussian.rs:321 */
+#define FOCK_SIGN_STANDARD 1  /* phi ~ (r - A)^l */
+
+#define FOCK_PREC_FP64 0  /* plain: every quartet in FP64 */
+#define FOCK_PREC_MIXED 1 /* FP32 where Q_ab Q_cd < mixed_threshold, FP64 otherwise */
+
+#define FOCK_ERI_EXACT 0     /* accurate Boys, correct recursions (the product path) */
+#define FOCK_ERI_REFCOMPAT 1 /* reference Boys LUT + x-branch recursion defect + 1e-6 zeroing
+                                (boys/src/lib.rs:58-81, basis/src/utils.rs:98-104,
+                                electron_tensor.rs:134-155) on the dense-tensor path */
+
+#define FOCK_GUESS_GWH 0  /* 0.875 S_ij (H_ii + H_jj), scf/src/lib.rs:150-162 */
+#define FOCK_GUESS_CORE 1 /* F = H */
+
+#define FOCK_CONV_COMMUTATOR 0 /* max|FDS - SDF| < epsilon, scf/src/lib.rs:191-192,224 */
+#define FOCK_CONV_ENERGY 1     /* |E_k - E_{k-1}| < epsilon and max|FDS-SDF| < sqrt(epsilon) */
+
+typedef struct {
+  double x, y, z; /* bohr */
+  int Z;          /* nuclear charge = electron count (basis_set/src/atom.rs:35-43) */
+} fock_atom;
+
+typedef struct {
+  int l;               /* 0, 1 or 2 (Cartesian); an SP shell is passed as two shells */
+  int nprim;
+  int atom;            /* index into the atom array: centre of the shell */
+  const double* exps;  /* nprim exponents */
+  const double* coefs; /* nprim raw contraction coefficients (normalised inside) */
+} fock_shell;
+
+typedef struct {
+  int sign_convention;    /* FOCK_SIGN_*, applies to D, G, C and the ERI tensor */
+  int precision;          /* FOCK_PREC_* */
+  int eri_mode;           /* FOCK_ERI_* */
+  double schwarz_eps;     /* shell-quartet screening: skip Q_ab Q_cd < schwarz_eps (exact mode) */
+  double mixed_threshold; /* FOCK_PREC_MIXED: FP64 for Q_ab Q_cd >= mixed_threshold */
+  double prim_eps;        /* drop primitive pairs with |K_ab| below this */
+  int group_by_contraction; /* split ket lists by primitive-pair count (uniform warps) */
+  /* SCF */
+  int max_iters;
+  double epsilon;
+  int conv_mode;  /* FOCK_CONV_* */
+  int guess;      /* FOCK_GUESS_* */
+  int diis_len;   /* 16 (scf/src/lib.rs:197) */
+  int diis_start; /* 5  (scf/src/lib.rs:202) */
+  int energy_mode; /* 0: reference 1/2 tr(D_new (2H + G(D_old))) (scf/src/lib.rs:223);
+                      1: consistent 1/2 tr(D (2H + G(D))) */
+  int final_fp64;  /* FOCK_PREC_MIXED: one FP64 Fock build + energy on the converged density */
+  int device;      /* CUDA device ordinal */
+} fock_options;
+
+typedef struct {
+  double electronic_energy; /* HartreeFockResult::electronic_energy */
+  double total_energy;      /* HartreeFockResult::total_energy */
+  double nuclear_repulsion;
+  int iterations;           /* HartreeFockResult::iterations */
+  int converged;            /* 1 when the criterion was met before max_iters */
+  int n_electrons;          /* HartreeFockResult::n_electrons */
+  int n_basis;              /* HartreeFockResult::n_basis */
+  double* orbital_energies;   /* optional, caller-owned [n_basis] (HartreeFockResult::orbital_energies) */
+  double* density_matrix;     /* optional, caller-owned [n_basis^2] (HartreeFockResult::density_matrix) */
+  double* coefficient_matrix; /* optional, caller-owned [n_basis^2] (HartreeFockResult::coefficient_matrix) */
+  double scf_seconds;       /* wall time of the SCF (integrals + iterations) */
+  double fock_seconds;      /* summed device time of the Fock builds */
+  int fock_builds;
+} fock_scf_result;
+
+typedef struct fock_ctx fock_ctx;
+
+/* Defaults: reference sign convention, FP64, exact ERIs, schwarz 1e-12,
+ * mixed threshold 1e-4, prim_eps 1e-20, grouping on, SCF 100 iterations,
+ * epsilon 1e-6, commutator convergence, GWH guess, DIIS 16/5, energy_mode 0. */
+void fock_options_default(fock_options* opt);
+
+/* Build shell pairs and primitive-pair data, Schwarz factors and the
+ * class-sorted quartet lists on the device.  Replaces the setup half of
+ * ElectronTensor::from_basis (electron_tensor.rs:81-101). */
+int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell,
+                    const fock_options* opt, fock_ctx** out);
+void fock_ctx_destroy(fock_ctx* ctx);
+int fock_nbasis(const fock_ctx* ctx);
+
+/* Re-plan the quartet lists with new thresholds (precision / schwarz / mixed). */
+int fock_set_precision(fock_ctx* ctx, int precision, double mixed_threshold);
+
+/* Full symmetric N^4 tensor, out[((l*N + k)*N + j)*N + i] = (ij|kl), so that
+ * out is indexed like ElectronTensor's Index (electron_tensor.rs:179-187).
+ * Debug / parity path; N <= 160. */
+int fock_eri_tensor(fock_ctx* ctx, double* out_n4);
+
+/* G = J - K/2 for a symmetric density D (host arrays), the two-electron part
+ * of F = H + G (scf/src/lib.rs:177-187), integral-direct: no N^4 storage. */
+int fock_build_jk(fock_ctx* ctx, const double* D, double* G);
+
+/* Same on device pointers (textbook sign convention, no host copies), queued
+ * on the context's stream.  Used by the device SCF and the benchmarks. */
+int fock_build_jk_device(fock_ctx* ctx, const double* D_dev, double* G_dev);
+
+/* S, T, V (nuclear attraction) in the selected sign convention
+ * (contracted_gaussian.rs:209-262). */
+int fock_one_electron(fock_ctx* ctx, double* S, double* T, double* V);
+
+/* Restricted Hartree-Fock with device-resident FP64 linear algebra
+ * (try_scf, scf/src/lib.rs:73-258).  Returns FOCK_OK (also when the
+ * iteration limit was reached: result->converged tells), or
+ * FOCK_ERR_DIVERGED when the DIIS error stops being a normal number
+ * (the reference's None). */
+int fock_scf(fock_ctx* ctx, int charge, fock_scf_result* result);
+
+/* Use an external CUDA stream (cudaStream_t) for all work of this context;
+ * NULL restores the context's own stream. */
+int fock_set_stream(fock_ctx* ctx, void* stream);
+
+/* Number of kernel launches issued by this context since creation. */
+long long fock_launch_count(const fock_ctx* ctx);
+
+/* Work statistics of the current quartet plan. */
+typedef struct {
+  long long shell_pairs;
+  long long prim_pairs;
+  long long shell_quartets_fp64;
+  long long shell_quartets_fp32;
+  long long prim_quartets_fp64;
+  long long prim_quartets_fp32;
+  long long shell_quartets_screened;
+  long long function_quartets_unique; /* N(N+1)/2 (N(N+1)/2 + 1)/2 */
+  long long flops_fp64;  /* algorithmic FP64 flops of one Fock build (model) */
+  long long flops_fp32;
+  int launches_per_build;
+} fock_stats;
+int fock_get_stats(const fock_ctx* ctx, fock_stats* st);
+
+const char* fock_strerror(int code);
+
+/* FP64 / FP32 FMA-pipe throughput microbenchmark on this device: fills
+ * *gflops with the measured rate (2 flops per FMA). */
+int fock_measure_fma_peak(int device, int fp64, double* gflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FOCK_GB300_H */

@@ -1,0 +1,105 @@
+"""Host-side logic and the C ABI surface: no CUDA device needed."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fock_gb300 import basis as B
+from fock_gb300 import molecules as M
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "fock_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fock_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol(gpu_lib):
+    names = header_functions()
+    assert len(names) >= 14
+    for name in names:
+        assert hasattr(gpu_lib, name), name
+
+
+def test_options_defaults_match_reference_constants(gpu_lib):
+    from fock_gb300 import options
+    o = options()
+    assert (o.diis_len, o.diis_start) == (16, 5)          # scf/src/lib.rs:197,202
+    assert o.guess == 0 and o.conv_mode == 0               # GWH, commutator
+    assert o.sign_convention == 0 and o.precision == 0
+
+
+def test_invalid_input_returns_codes_not_abort(gpu_lib):
+    from fock_gb300 import _lib as L
+    atoms = (L.Atom * 1)(L.Atom(0, 0, 0, 1))
+    e = np.array([1.0])
+    c = np.array([1.0])
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    h = C.c_void_p()
+    sh = (L.Shell * 1)(L.Shell(3, 1, 0, dp(e), dp(c)))
+    assert gpu_lib.fock_ctx_create(atoms, 1, sh, 1, None, C.byref(h)) == -2  # UNSUPPORTED_L
+    sh = (L.Shell * 1)(L.Shell(0, 1, 5, dp(e), dp(c)))
+    assert gpu_lib.fock_ctx_create(atoms, 1, sh, 1, None, C.byref(h)) == -1  # bad atom index
+    bad = np.array([-1.0])
+    sh = (L.Shell * 1)(L.Shell(0, 1, 0, dp(bad), dp(c)))
+    assert gpu_lib.fock_ctx_create(atoms, 1, sh, 1, None, C.byref(h)) == -1  # non-positive exponent
+    assert gpu_lib.fock_ctx_create(atoms, 0, sh, 1, None, C.byref(h)) == -1
+    assert gpu_lib.fock_strerror(-5) == b"SCF diverged (DIIS error not a normal number)"
+
+
+@pytest.mark.parametrize("name,basis,nbf,nel", [
+    ("h2o", "STO-3G", 7, 10), ("benzene", "6-31G", 66, 42), ("octane", "6-31G", 108, 66),
+    ("water32", "6-31G*", 608, 320)])
+def test_workload_sizes(name, basis, nbf, nel):
+    gen = {"h2o": M.water_sto3g, "benzene": M.benzene, "octane": M.octane,
+           "water32": lambda: M.water_cluster(32, seed=0)}[name]
+    Zs, xyz = gen()
+    atoms = B.build_atoms(basis, Zs, xyz)
+    assert B.n_basis(atoms) == nbf
+    assert sum(Zs) == nel
+
+
+def test_reference_function_order():
+    # p = (z, y, x), d = (zz, yz, yy, xz, xy, xx): basis_set/src/lib.rs:88-100
+    assert B.cartesian_components(1) == [(0, 0, 1), (0, 1, 0), (1, 0, 0)]
+    assert B.cartesian_components(2) == [(0, 0, 2), (0, 1, 1), (0, 2, 0), (1, 0, 1), (1, 1, 0), (2, 0, 0)]
+    atoms = B.build_atoms("6-31G", [8], [[0, 0, 0]])
+    assert [s.l for s in atoms[0].shells] == [0, 0, 1, 0, 1]  # SP shells split into s + p
+
+
+def test_water_cluster_recipe():
+    for n in (1, 4, 8):
+        Zs, xyz = M.water_cluster(n, seed=n)
+        oxy = xyz[0::3] / B.ANGSTROM_TO_BOHR
+        for i in range(n):
+            oh = np.linalg.norm(xyz[3 * i + 1] - xyz[3 * i]) / B.ANGSTROM_TO_BOHR
+            assert abs(oh - 0.957) < 1e-9
+            for j in range(i):
+                assert np.linalg.norm(oxy[i] - oxy[j]) >= 2.6
+    batch = M.water_cluster_batch(512, seed=0)
+    sizes = [len(z) // 3 for z, _ in batch]
+    assert len(batch) == 512 and min(sizes) == 1 and max(sizes) == 8
+
+
+def test_octane_geometry():
+    Zs, xyz = M.octane(seed=0, sigma=0.0)
+    xyz = xyz / B.ANGSTROM_TO_BOHR
+    c = xyz[:8]
+    for k in range(7):
+        assert abs(np.linalg.norm(c[k + 1] - c[k]) - 1.53) < 1e-9
+    hs = xyz[8:]
+    assert len(hs) == 18
+    for h in hs:
+        assert abs(np.min(np.linalg.norm(c - h, axis=1)) - 1.09) < 1e-9
+
+
+def test_xyz_reader_uses_reference_factor(tmp_path):
+    p = tmp_path / "w.xyz"
+    p.write_text("3\nwater\nO 0.0 0.0 0.117\nH 0.0 0.757 -0.469\nH 0.0 -0.757 -0.469\n")
+    atoms = B.read_xyz(str(p), "STO-3G")
+    assert abs(atoms[1].position[1] - 0.757 * 1.89) < 1e-12

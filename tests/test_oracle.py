@@ -1,0 +1,164 @@
+"""The CPU oracle against the reference's golden vector, mpmath, an
+independent Python restatement of the reference (tests/golden), closed forms
+and invariances.  No GPU needed."""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from fock_gb300 import basis as B
+from fock_gb300 import molecules as M
+
+REF = "/root/reference"
+
+
+def test_hermite_expansion_doctest_golden(oracle_lib):
+    # basis/src/utils.rs:24 (the reference's only golden value), exact equality
+    assert oracle_lib.hermite_expansion(1, 2, 3, 2.5, 3.0, 5.0) == 1.9872458203327215e-9
+
+
+def test_boys_exact_vs_mpmath(oracle_lib, golden_boys):
+    worst = 0.0
+    for row in golden_boys["rows"]:
+        t = row[0]
+        for n in range(golden_boys["orders"]):
+            ref = row[1 + n]
+            got = oracle_lib.boys(t, n, oracle_lib.EXACT)
+            err = abs(got - ref) / max(abs(ref), 1e-300)
+            worst = max(worst, err)
+    assert worst < 5e-14, worst
+
+
+def test_boys_reference_lut_matches_reference_file(oracle_lib):
+    path = os.path.join(REF, "boys/src/lut.rs")
+    if not os.path.exists(path):
+        pytest.skip("reference sources not present")
+    import re
+    src = open(path).read()
+    lut = [float(x) for x in re.findall(r"[-+0-9.eE]+(?=,)", src.split("=", 1)[1])]
+    ours = [oracle_lib.lib().orc_boys_lut_entry(k) for k in range(200)]
+    rel = max(abs(a - b) / abs(b) for a, b in zip(ours, lut))
+    # the reference's table came from a quadrature crate; ours is the exact F_10
+    assert rel < 1e-11, rel
+
+
+def test_boys_reference_behaviour(oracle_lib):
+    # reference quirks: exact 1/(2n+1) at t=0, asymptotic formula from t=30 on,
+    # relative error of the interpolated range up to ~1e-3 (loose by design)
+    assert oracle_lib.boys(0.0, 3, oracle_lib.BOYS_LUT) == 1.0 / 7.0
+    for t in (30.0, 45.0):
+        for n in range(6):
+            a = oracle_lib.boys(t, n, oracle_lib.BOYS_LUT)
+            b = oracle_lib.boys(t, n, oracle_lib.EXACT)
+            assert abs(a - b) <= 1e-14
+    errs = [abs(oracle_lib.boys(t, 0, oracle_lib.BOYS_LUT) - oracle_lib.boys(t, 0, 0)) for t in np.linspace(0.01, 29, 50)]
+    assert 1e-9 < max(errs) < 1e-2
+
+
+@pytest.fixture(scope="module")
+def h2o(oracle_lib):
+    Zs, xyz = M.water_sto3g()
+    atoms = B.build_atoms("STO-3G", Zs, xyz)
+    return atoms, oracle_lib.OracleBasis(atoms)
+
+
+def test_oracle_eris_vs_python_restatement(oracle_lib, h2o, golden_h2o):
+    atoms, ob = h2o
+    for mode, flags, tol in (("exact", oracle_lib.EXACT, 1e-12), ("refcompat", oracle_lib.REFCOMPAT, 1e-10)):
+        vals = golden_h2o["modes"][mode]["eri"]
+        worst = 0.0
+        for (i, j, k, l), v in zip(golden_h2o["quartets"], vals):
+            worst = max(worst, abs(oracle_lib.eri(ob, i, j, k, l, flags) - v))
+        assert worst < tol, (mode, worst)
+
+
+def test_oracle_recursive_equals_tabulated(oracle_lib, h2o):
+    atoms, ob = h2o
+    a = oracle_lib.eri_tensor(ob, oracle_lib.REFCOMPAT | oracle_lib.RECURSIVE)
+    b = oracle_lib.eri_tensor(ob, oracle_lib.REFCOMPAT)
+    assert np.abs(a - b).max() < 1e-14
+
+
+def test_oracle_one_electron_vs_python_restatement(oracle_lib, h2o, golden_h2o):
+    atoms, ob = h2o
+    for mode, flags in (("exact", oracle_lib.EXACT), ("refcompat", oracle_lib.REFCOMPAT)):
+        S, T, V = oracle_lib.one_electron(ob, flags)
+        g = golden_h2o["modes"][mode]
+        assert np.abs(S - np.array(g["S"])).max() < 1e-13
+        assert np.abs(T - np.array(g["T"])).max() < 1e-12
+        assert np.abs(V - np.array(g["V"])).max() < 1e-11
+
+
+def test_oracle_scf_vs_python_restatement(oracle_lib, h2o, golden_h2o):
+    atoms, ob = h2o
+    for mode, flags in (("exact", oracle_lib.EXACT), ("refcompat", oracle_lib.REFCOMPAT)):
+        r, D, eps = oracle_lib.scf(ob, max_iters=100, epsilon=1e-6, eri_flags=flags,
+                                   schwarz=1e-6 if mode == "refcompat" else -1.0)
+        g = golden_h2o["modes"][mode]
+        assert r.iterations == g["iterations"]
+        assert abs(r.total_energy - g["total_energy"]) < 1e-9, (mode, r.total_energy, g["total_energy"])
+
+
+def test_ss_closed_form(oracle_lib):
+    # (ss|ss) over single normalised primitives: 2 pi^(5/2)/(pq sqrt(p+q)) K_ab K_cd F0(T)
+    from scipy.special import erf
+    xyz = np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.4], [0.3, -0.2, 2.9], [1.1, 0.7, -0.4]])
+    atoms = []
+    for i, e in enumerate((0.8, 1.3, 0.5, 2.1)):
+        a = B.Atom(xyz[i], 1)
+        a.shells.append(B.Shell(0, i, xyz[i], np.array([e]), np.array([1.0])))
+        atoms.append(a)
+    ob = oracle_lib.OracleBasis(atoms)
+    a, b, c, d = 0.8, 1.3, 0.5, 2.1
+    N = [(2 * e / math.pi) ** 0.75 for e in (a, b, c, d)]
+    p, q = a + b, c + d
+    P = (a * xyz[0] + b * xyz[1]) / p
+    Q = (c * xyz[2] + d * xyz[3]) / q
+    Kab = math.exp(-a * b / p * np.sum((xyz[0] - xyz[1]) ** 2))
+    Kcd = math.exp(-c * d / q * np.sum((xyz[2] - xyz[3]) ** 2))
+    T = p * q / (p + q) * np.sum((P - Q) ** 2)
+    F0 = 0.5 * math.sqrt(math.pi / T) * erf(math.sqrt(T))
+    ref = 2 * math.pi ** 2.5 / (p * q * math.sqrt(p + q)) * Kab * Kcd * F0 * N[0] * N[1] * N[2] * N[3]
+    assert abs(oracle_lib.eri(ob, 0, 1, 2, 3, oracle_lib.EXACT) - ref) < 1e-14
+
+
+def test_eri_symmetry_translation_sign(oracle_lib):
+    Zs, xyz = M.water_sto3g()
+    atoms = B.build_atoms("STO-3G", Zs, xyz)
+    ob = oracle_lib.OracleBasis(atoms)
+    n = ob.n
+    t = oracle_lib.eri_tensor(ob, oracle_lib.EXACT).reshape(n, n, n, n)  # t[l,k,j,i] = (ij|kl)
+    for perm in ((1, 0, 2, 3), (0, 1, 3, 2), (2, 3, 0, 1)):
+        assert np.abs(t - t.transpose(perm)).max() < 1e-15
+    shifted = B.build_atoms("STO-3G", Zs, xyz + np.array([0.37, -1.2, 2.5]))
+    t2 = oracle_lib.eri_tensor(oracle_lib.OracleBasis(shifted), oracle_lib.EXACT).reshape(n, n, n, n)
+    assert np.abs(t - t2).max() < 1e-12
+    # textbook vs reference convention: factor (-1)^(l_i + l_j + l_k + l_l)
+    ts = oracle_lib.eri_tensor(ob, oracle_lib.EXACT | oracle_lib.STANDARD_SIGN).reshape(n, n, n, n)
+    s = B.reference_sign_vector(atoms)
+    assert np.abs(ts - t * np.einsum("i,j,k,l->lkji", s, s, s, s)).max() < 1e-15
+
+
+def test_direct_g_equals_tensor_g(oracle_lib):
+    from conftest import random_density
+    Zs, xyz = M.water_cluster(2, seed=3)
+    atoms = B.build_atoms("6-31G*", Zs, xyz)
+    ob = oracle_lib.OracleBasis(atoms)
+    D = random_density(ob.n, 1)
+    G1 = oracle_lib.jk(ob, D, oracle_lib.EXACT)
+    G2 = oracle_lib.g_from_tensor(oracle_lib.eri_tensor(ob, oracle_lib.EXACT), D)
+    assert np.abs(G1 - G2).max() < 1e-12
+
+
+def test_energy_rotation_invariance(oracle_lib):
+    Zs, xyz = M.water_sto3g()
+    th = 0.7
+    R = np.array([[math.cos(th), -math.sin(th), 0], [math.sin(th), math.cos(th), 0], [0, 0, 1]])
+    e = []
+    for X in (xyz, xyz @ R.T):
+        ob = oracle_lib.OracleBasis(B.build_atoms("STO-3G", Zs, X))
+        r, _, _ = oracle_lib.scf(ob, max_iters=100, epsilon=1e-10, eri_flags=oracle_lib.EXACT, guess=1, conv=1,
+                                 energy_mode=1, schwarz=-1.0)
+        e.append(r.total_energy)
+    assert abs(e[0] - e[1]) < 1e-9
