@@ -1,0 +1,343 @@
+"""Benchmark of the ERI + Fock (J/K) build on one GB300.
+
+Workload: benzene C6H6 RHF/6-31G (D6h, C-C 1.39 A, C-H 1.09 A), 66 basis
+functions, 2,445,366 unique contracted function quartets.  One step = one
+integral-direct Fock build G = J - K/2 from a density resident in HBM (the
+converged SCF density of the molecule).
+
+Metric: ERI+Fock quartets/s = unique function quartets / build time (screened
+quartets count in the numerator for every path), plus the SCF wall time.
+``value`` is the plain FP64 path (the drop-in); the mixed FP32/FP64 path and
+its energy error against the FP64 result are reported beside it.
+
+Timing: W warm-up builds, then K builds, each bracketed by CUDA events on the
+stream the library launches on; between builds a 256 MB buffer is written to
+flush the 129 MB L2 (outside the events).  ``e2e`` times the C-ABI call with
+host buffers (fock_build_jk: H2D of D, build, D2H of G).
+
+``--impl reference`` times the reference's algorithm (the CPU restatement in
+oracle/: recursive E/R, per-function primitive loops, dense N^4 tensor with
+1e-6 zeroing, serial electron_terms + G loops) on all host cores, on a
+bounded sample of the outer w loop.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fock-rs_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import numpy as np  # noqa: E402
+
+METRIC = "ERI+Fock quartets/s (C6H6 RHF/6-31G Fock build)"
+UNIT = "quartets/s"
+WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
+            "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def benzene_atoms():
+    from fock_gb300 import basis as B
+    from fock_gb300 import molecules as M
+    Zs, xyz = M.benzene()
+    return B.build_atoms("6-31G", Zs, xyz)
+
+
+def cpu_reference(steps, warmup, sample_w=3, threads=0):
+    """Reference algorithm on the host cores; one step = the sampled outer-w
+    iterations of from_basis + the full electron_terms and G loops."""
+    import oracle
+    oracle.build()
+    atoms = benzene_atoms()
+    ob = oracle.OracleBasis(atoms)
+    n = ob.n
+    rng = np.random.default_rng(0)
+    Cm = rng.normal(size=(n, 21)) / np.sqrt(n)
+    D = 2.0 * Cm @ Cm.T
+    nthreads = threads or oracle.max_threads()
+    stride = max(1, n // sample_w)
+    rates, tf_all = [], []
+    total_unique = WORKLOAD["unique_quartets"]
+    for it in range(warmup + steps):
+        w0 = (it * 7) % stride
+        cnt, te, tf = oracle.ref_build_timed(ob, D, oracle.REFCOMPAT, w_begin=w0, w_stride=stride,
+                                             full_fock=(it == warmup), threads=nthreads)
+        if it >= warmup:
+            rates.append(cnt / te)
+            if tf > 0:
+                tf_all.append(tf)
+    rate = statistics.median(rates)
+    t_eri = total_unique / rate
+    t_fock = tf_all[0] if tf_all else 0.0
+    value = total_unique / (t_eri + t_fock)
+    return value, {"kind": "port", "cores": nthreads,
+                   "sample": "outer-w iterations w0, w0+%d, ... of from_basis (about 1/%d of the quartets) per step, "
+                             "literal recursive E/R, 1e-6 zeroing; electron_terms + G loops timed in full once "
+                             "(%.2f s); full-build time extrapolated by quartet count" % (stride, stride, t_fock),
+                   "eri_quartets_per_s": rate, "est_full_build_s": t_eri + t_fock}
+
+
+def run_reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    value, cb = cpu_reference(args.steps, args.warmup)
+    cb["value"] = value
+    cb["unit"] = UNIT
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * WORKLOAD["unique_quartets"] / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": WORKLOAD, "cpu_baseline": cb,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scf", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    import fock_gb300 as F
+    from fock_gb300 import _lib as L
+    atoms = benzene_atoms()
+    opts = dict(guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, device=local,
+                sign_convention=L.FOCK_SIGN_STANDARD)
+    extra = {}
+    # converged density (FP64 SCF) for the benchmark builds; SCF wall times
+    t0 = time.perf_counter()
+    r64 = F.try_scf(atoms, 100, 1e-9, 0, **opts)
+    scf64_s = time.perf_counter() - t0
+    rmx = None
+    if not args.no_scf:
+        t0 = time.perf_counter()
+        rmx = F.try_scf(atoms, 100, 1e-9, 0, precision=L.FOCK_PREC_MIXED, mixed_threshold=1e-4, **opts)
+        scfmx_s = time.perf_counter() - t0
+        extra["scf"] = {"fp64_wall_s": scf64_s, "fp64_iterations": r64.iterations, "fp64_energy": r64.total_energy,
+                        "fp64_fock_builds": r64.fock_builds, "fp64_fock_s": r64.fock_seconds,
+                        "mixed_wall_s": scfmx_s, "mixed_iterations": rmx.iterations,
+                        "mixed_energy": rmx.total_energy, "mixed_fock_s": rmx.fock_seconds,
+                        "abs_energy_error_mixed_vs_fp64_eh": abs(rmx.total_energy - r64.total_energy)}
+    ctx = F.FockContext(atoms, **opts)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    n = ctx.n
+    D = torch.tensor(r64.density_matrix, dtype=torch.float64, device="cuda")
+    G = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    nq = WORKLOAD["unique_quartets"]
+
+    def timed_builds(k, w):
+        with torch.cuda.stream(stream):
+            for _ in range(w):
+                ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+            for e0, e1 in ev:
+                flush.fill_(1.0)
+                e0.record(stream)
+                ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+                e1.record(stream)
+        stream.synchronize()
+        return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+    # ---- plain FP64 (headline) ----
+    clocks = ClockSampler(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    clocks.start()
+    times = timed_builds(args.steps, args.warmup)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = ctx.launch_count() - l0
+    ms = sum(times) / len(times)
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * nq / (ms_max * 1e-3)
+    st = ctx.stats()
+
+    # ---- per-launch profile -> dominant kernel roofline ----
+    from fock_gb300 import _lib
+    cap = 512
+
+    class Prof(C.Structure):
+        _fields_ = [("la", C.c_int), ("lb", C.c_int), ("lc", C.c_int), ("ld", C.c_int), ("prec", C.c_int),
+                    ("quartets", C.c_longlong), ("prim_quartets", C.c_longlong), ("flops", C.c_longlong),
+                    ("ms", C.c_float)]
+    arr = (Prof * cap)()
+    lib = _lib.lib()
+    lib.fock_profile_build.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Prof), C.c_int]
+    per_class = {}
+    for _ in range(3):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        np_ = lib.fock_profile_build(ctx.handle, C.c_void_p(D.data_ptr()), arr, cap)
+        for i in range(min(np_, cap)):
+            a = arr[i]
+            key = "(%d%d|%d%d)%s" % (a.la, a.lb, a.lc, a.ld, "" if a.prec == 0 else "f32")
+            d = per_class.setdefault(key, {"ms": 0.0, "flops": 0, "launches": 0, "prim_quartets": 0})
+            d["ms"] += a.ms / 3.0
+            d["flops"] += a.flops // 3
+            d["launches"] += 1
+            d["prim_quartets"] += a.prim_quartets // 3
+    for d in per_class.values():
+        d["launches"] //= 3
+    total_ms = sum(d["ms"] for d in per_class.values())
+    dom_key = max(per_class, key=lambda k: per_class[k]["ms"])
+    dom = per_class[dom_key]
+    fp64_peak_gflops = C.c_double()
+    lib.fock_measure_fma_peak(local, 1, C.byref(fp64_peak_gflops))
+    fp32_peak_gflops = C.c_double()
+    lib.fock_measure_fma_peak(local, 0, C.byref(fp32_peak_gflops))
+    achieved = dom["flops"] / (dom["ms"] * 1e-3) / 1e12
+    peak = fp64_peak_gflops.value / 1e3
+    build_flops = st["flops_fp64"]
+    roofline = {"bound": "fp64_pipe", "kernel": "eri_kernel %s" % dom_key, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if peak else None, "traffic": None,
+                "peak_source": "measured FP64 FMA microbenchmark in this run (fock_measure_fma_peak)",
+                "share_of_build": dom["ms"] / total_ms if total_ms else None,
+                "whole_build": {"flops": build_flops, "achieved": build_flops / (ms * 1e-3) / 1e12,
+                                "frac": build_flops / (ms * 1e-3) / 1e12 / peak if peak else None},
+                "fp32_peak_tflops": fp32_peak_gflops.value / 1e3,
+                "per_class_ms": {k: round(v["ms"], 4) for k, v in sorted(per_class.items())}}
+
+    # ---- mixed precision build ----
+    ctx.set_precision(L.FOCK_PREC_MIXED, 1e-4)
+    tmx = timed_builds(args.steps, args.warmup)
+    ms_mx = sum(tmx) / len(tmx)
+    stm = ctx.stats()
+    Gm = G.clone()
+    ctx.set_precision(L.FOCK_PREC_FP64, 1e-4)
+    ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+    stream.synchronize()
+    mixed = {"value": nq / (ms_mx * 1e-3), "ms_per_step": ms_mx, "speedup_vs_fp64": ms / ms_mx,
+             "mixed_threshold": 1e-4, "fp32_shell_quartets": stm["shell_quartets_fp32"],
+             "fp64_shell_quartets": stm["shell_quartets_fp64"],
+             "max_abs_fock_error_vs_fp64": float((Gm - G).abs().max().item())}
+    if rmx is not None:
+        mixed["abs_energy_error_vs_fp64_eh"] = abs(rmx.total_energy - r64.total_energy)
+
+    # ---- e2e through the C ABI with host buffers ----
+    Dh = np.ascontiguousarray(r64.density_matrix)
+    ctx.set_stream(0)
+    for _ in range(args.warmup):
+        ctx.build_jk(Dh)
+    te = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.build_jk(Dh)
+        te.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(te)
+    e2e = {"value": world * nq / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": n * n * 8,
+           "ms_per_step": e2e_s * 1e3, "api": "fock_build_jk (host D in, host G out)"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            v, cb = cpu_reference(1, 0)
+            cb["value"] = v
+            cb["unit"] = UNIT
+            cpu = cb
+        except Exception as ex:  # baseline is reported, never fatal
+            cpu = {"value": None, "error": str(ex)[:200]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single"),
+                "clocks": clk, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
+                "mixed": mixed, "stats": {k: st[k] for k in ("shell_quartets_fp64", "prim_quartets_fp64",
+                                                               "shell_quartets_screened", "launches_per_build")}}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

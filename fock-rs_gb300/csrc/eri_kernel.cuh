@@ -122,7 +122,7 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
       const R rq = bp.p * inv;   // rho / q
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const R r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
-      const R T = kp.p * rp * r2;  // rho |PQ|^2
+      const R T = bp.p * rp * r2;  // rho |PQ|^2, rho = p q / (p + q)
       const R pref = bp.K * kp.K * rs;
       R F[L + 1];
       boys_scaled<L>(T, pref, btab, a.exp64, F);

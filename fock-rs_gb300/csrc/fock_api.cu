@@ -112,7 +112,7 @@ struct HostShell {
 struct Plan {
   int la, lb, lc, ld, prec;
   ClassLaunch cl;
-  long long quartets, prim_quartets;
+  long long quartets, prim_quartets, flops;
 };
 
 int map_cuda(cudaError_t e) {
@@ -256,7 +256,15 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   st.prim_pairs = c->nprim_pairs;
   const long long nfp = (long long)c->nbf * (c->nbf + 1) / 2;
   st.function_quartets_unique = nfp * (nfp + 1) / 2;
+  // every shell quartet of the basis (pairs whose primitive pairs were all
+  // dropped count as screened)
   long long total_shell_quartets = 0;
+  {
+    std::vector<long long> ncls(kNumPairClasses, 0);
+    for (const PairInfo& p : c->hpairs) ncls[p.cls]++;
+    for (int X = 0; X < kNumPairClasses; ++X)
+      for (int Y = 0; Y <= X; ++Y) total_shell_quartets += (X == Y) ? ncls[X] * (ncls[X] + 1) / 2 : ncls[X] * ncls[Y];
+  }
   for (int X = 0; X < kNumPairClasses; ++X) {
     if (cls[X].empty()) continue;
     for (int Y = 0; Y <= X; ++Y) {
@@ -269,8 +277,6 @@ int build_plan(fock_ctx* c, bool for_tensor) {
         }
       const std::vector<int>& bras = cls[X];
       const std::vector<int>& kall = cls[Y];
-      total_shell_quartets += (X == Y) ? (long long)bras.size() * (bras.size() + 1) / 2
-                                       : (long long)bras.size() * kall.size();
       // ket groups (by primitive-pair count) keep the Q order
       std::vector<std::vector<int>> groups;
       if (c->opt.group_by_contraction) {
@@ -354,6 +360,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           P.p.cl.nwarps = acc;
           pend.push_back(P);
           const long long flops = pq * ((long long)vrr + setup_flops(L)) + q * ((long long)hrr + 12LL * neri);
+          pend.back().p.flops = flops;
           if (P.p.prec == PREC_FP32) {
             st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
           } else {
@@ -701,6 +708,39 @@ int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
   CK(k_symmetrize(c->d_M, G_dev, n, c->stream));
   c->launches++;
   return FOCK_OK;
+}
+
+int fock_profile_build(fock_ctx* c, const double* D_dev, fock_launch_profile* out, int cap) {
+  if (!c || !D_dev || (cap > 0 && !out)) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  const size_t nn = (size_t)c->nbf * c->nbf;
+  CK(cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), c->stream));
+  EriArgs a = eri_args(c);
+  a.D = D_dev;
+  CK(k_to_float(D_dev, c->d_D32, (int)nn, c->stream));
+  c->launches++;
+  const int np = (int)c->plans.size();
+  std::vector<cudaEvent_t> ev(2 * (size_t)np);
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  cudaError_t err = cudaSuccess;
+  for (int i = 0; i < np && err == cudaSuccess; ++i) {
+    const Plan& p = c->plans[i];
+    cudaEventRecord(ev[2 * i], c->stream);
+    err = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->stream);
+    c->launches++;
+    cudaEventRecord(ev[2 * i + 1], c->stream);
+  }
+  if (err == cudaSuccess) err = cudaStreamSynchronize(c->stream);
+  for (int i = 0; i < np && i < cap && err == cudaSuccess; ++i) {
+    const Plan& p = c->plans[i];
+    fock_launch_profile& o = out[i];
+    o.la = p.la; o.lb = p.lb; o.lc = p.lc; o.ld = p.ld; o.prec = p.prec;
+    o.quartets = p.quartets; o.prim_quartets = p.prim_quartets; o.flops = p.flops;
+    cudaEventElapsedTime(&o.ms, ev[2 * i], ev[2 * i + 1]);
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  CK(err);
+  return np;
 }
 
 int fock_build_jk(fock_ctx* c, const double* D, double* G) {

@@ -172,6 +172,17 @@ typedef struct {
 } fock_stats;
 int fock_get_stats(const fock_ctx* ctx, fock_stats* st);
 
+/* Per-launch profile of one Fock build from a device density: every class
+ * launch runs alone between CUDA events on the context stream.  Fills up to
+ * cap entries and returns the number of launches (or a negative code). */
+typedef struct {
+  int la, lb, lc, ld; /* angular class (la lb | lc ld) */
+  int prec;           /* FOCK_PREC_FP64 (0) or FP32 quartets (1) */
+  long long quartets, prim_quartets, flops; /* flops: algorithmic model of the recurrences */
+  float ms;           /* device time of the launch */
+} fock_launch_profile;
+int fock_profile_build(fock_ctx* ctx, const double* D_dev, fock_launch_profile* out, int cap);
+
 const char* fock_strerror(int code);
 
 /* FP64 / FP32 FMA-pipe throughput microbenchmark on this device: fills
