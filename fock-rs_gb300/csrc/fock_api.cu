@@ -710,6 +710,38 @@ int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
   return FOCK_OK;
 }
 
+}  // extern "C"
+
+// Fock build with caller-provided working memory (accumulator M and the FP32
+// density copy), used by the allocation-free entry point in noalloc.cu.
+int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, double* M, float* D32) {
+  const int n = c->nbf;
+  const size_t nn = (size_t)n * n;
+  CK(cudaMemsetAsync(M, 0, nn * sizeof(double), c->stream));
+  EriArgs a = eri_args(c);
+  a.D = D_dev;
+  a.D32 = D32;
+  a.M = M;
+  bool need32 = false;
+  for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
+  if (need32) {
+    CK(k_to_float(D_dev, D32, (int)nn, c->stream));
+    c->launches++;
+  }
+  for (const Plan& p : c->plans) {
+    cudaError_t e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->stream);
+    c->launches++;
+    CK(e);
+  }
+  CK(k_symmetrize(M, G_dev, n, c->stream));
+  c->launches++;
+  return FOCK_OK;
+}
+
+int fockgb_ctx_device(const fock_ctx* c) { return c->device; }
+
+extern "C" {
+
 int fock_profile_build(fock_ctx* c, const double* D_dev, fock_launch_profile* out, int cap) {
   if (!c || !D_dev || (cap > 0 && !out)) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));

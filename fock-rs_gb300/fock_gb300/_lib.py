@@ -80,6 +80,7 @@ def lib():
         L.fock_eri_tensor.argtypes = [vp, dp]
         L.fock_build_jk.argtypes = [vp, dp, dp]
         L.fock_build_jk_device.argtypes = [vp, vp, vp]
+        L.fock_build_jk_noalloc.argtypes = [vp, vp, vp]
         L.fock_one_electron.argtypes = [vp, dp, dp, dp]
         L.fock_scf.argtypes = [vp, C.c_int, C.POINTER(ScfResult)]
         L.fock_set_stream.argtypes = [vp, vp]

@@ -138,6 +138,24 @@ int fock_build_jk(fock_ctx* ctx, const double* D, double* G);
  * on the context's stream.  Used by the device SCF and the benchmarks. */
 int fock_build_jk_device(fock_ctx* ctx, const double* D_dev, double* G_dev);
 
+/* Allocation-free variant of fock_build_jk_device (no counterpart in the
+ * reference).  For callers that create their context up front but must run
+ * Fock builds where no device memory can be obtained: for example a host
+ * framework that has handed the free device memory to its own pool, or a
+ * service at its memory limit.  The call never allocates or frees.  Its
+ * working memory (J/K accumulator, FP32 density copy) is a fixed array in the
+ * library's device image.  That array is held by every GPU that loads the
+ * library, until the process exits.
+ *   - n_basis <= FOCK_NOALLOC_MAX_BASIS, else FOCK_ERR_TOO_LARGE;
+ *   - the first call on a device looks up the array's device address; make
+ *     that first call before any stream capture on that device;
+ *   - all calls on a device share the array: calls whose GPU work overlaps
+ *     (other streams, contexts or threads) race and corrupt each other.
+ * Inputs and outputs as fock_build_jk_device (device pointers, textbook sign
+ * convention, queued on the context's stream). */
+#define FOCK_NOALLOC_MAX_BASIS 256
+int fock_build_jk_noalloc(fock_ctx* ctx, const double* D_dev, double* G_dev);
+
 /* S, T, V (nuclear attraction) in the selected sign convention
  * (contracted_gaussian.rs:209-262). */
 int fock_one_electron(fock_ctx* ctx, double* S, double* T, double* V);
