@@ -46,6 +46,7 @@ def _compile(src, verbose):
         return obj
     cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj,
                              "-I", CSRC, "--expt-relaxed-constexpr"]
+    cmd += os.environ.get("FOCK_GB300_NVCC_FLAGS", "").split()
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

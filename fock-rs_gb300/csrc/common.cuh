@@ -7,21 +7,25 @@ namespace fockgb {
 
 // ---------------------------------------------------------------------------
 // Boys-function tables.
-// F_n(T) is tabulated on T_i = i/16, i = 0..1024 (T < 64).  For every order M
-// a row holds the Taylor coefficients c_k = F_{M+k}(T_i) (-1)^k / k!, k = 0..7,
-// so F_M(T_i + d) = sum_k c_k d^k with |d| <= 1/32; truncation error
-// (1/32)^8 / 8! < 3e-17 relative.  exp(-T_i) is tabulated beside it for the
-// downward recursion F_{m-1} = (2T F_m + e^{-T}) / (2m - 1).  For T >= 64,
-// F_0 = sqrt(pi/T)/2 and F_m = F_{m-1} (2m-1)/(2T) (the neglected e^{-T} term
-// is below 1e-27 there).
+// F_n(T) is tabulated on T_i = i/32, i = 0..2048 (T < 64).  For every order M
+// a 64-byte row holds the Taylor coefficients c_k = F_{M+k}(T_i) (-1)^k / k!,
+// k = 0..6, and exp(-T_i) in slot 7, so that with d = T - T_i, |d| <= 1/64,
+//   F_M(T) = sum_k c_k d^k          (truncation (1/64)^7/7! < 5e-17 relative)
+//   e^{-T} = e^{-T_i} sum_k (-d)^k/k!, k <= 6 (same bound)
+// and lower orders follow by the downward recursion
+//   F_{m-1} = (2T F_m + e^{-T}) / (2m - 1).
+// For T >= 64, F_0 = sqrt(pi/T)/2 and F_m = F_{m-1} (2m-1)/(2T) (the neglected
+// e^{-T} terms are below 1e-27 there).
 // ---------------------------------------------------------------------------
-constexpr int kBoysPts = 1025;
-constexpr int kBoysTerms = 8;
+constexpr int kBoysPerUnit = 32;
+constexpr int kBoysPts = 64 * kBoysPerUnit + 1;
+constexpr int kBoysTerms = 8;           // 7 Taylor coefficients + exp(-T_i)
+constexpr int kBoysTaylor = 7;
 constexpr int kBoysMaxM = 12;           // orders with a Taylor table
 constexpr double kBoysTmax = 64.0;
 constexpr float kBoysTmaxF = 64.0f;
 
-enum Mode { MODE_JK = 0, MODE_TENSOR = 1, MODE_SCHWARZ = 2 };
+enum Mode { MODE_JK = 0, MODE_TENSOR = 1, MODE_SCHWARZ = 2, MODE_GRAD = 3 };
 enum Prec { PREC_FP64 = 0, PREC_FP32 = 1 };
 
 // Contracted shell pair (a, b), la >= lb (equal l: shell a >= shell b).
@@ -33,30 +37,46 @@ struct PairInfo {
   float Q;        // Schwarz factor sqrt(max |(ab|ab)|)
   int cls;        // pair class index
   double AB[3];   // A - B
-  double pad;
+  int atom_a, atom_b;  // centres of shells a and b (gradient)
 };
 
-// Primitive pair, double: {p, 1/(2p)}, {K, Px}, {Py, Pz}, {PAx, PAy}, {PAz, 0}
-// with K = c_a c_b exp(-ab/p |AB|^2) sqrt(2) pi^(5/4) / p, so that the ERI
+// Primitive pair, double: {p, 1/(2p)}, {K, Px}, {Py, Pz}, {PAx, PAy},
+// {PAz, exponent-sum id as integer bits}, {alpha (exponent of shell a), 0} with
+// K = c_a c_b exp(-ab/p |AB|^2) sqrt(2) pi^(5/4) / p, so that the ERI
 // prefactor 2 pi^(5/2) / (p q sqrt(p+q)) c_a c_b c_c c_d exp(..)exp(..) is
 // K_ab K_cd / sqrt(p+q).
 struct __align__(16) PrimPair64 {
-  double2 v[5];
+  double2 v[6];
 };
-// Primitive pair, float: {p, 1/(2p), K, Px}, {Py, Pz, PAx, PAy}, {PAz, 0, 0, 0}
+// Primitive pair, float: {p, 1/(2p), K, Px}, {Py, Pz, PAx, PAy}, {PAz, id bits, 0, 0}
 struct __align__(16) PrimPair32 {
   float4 v[3];
 };
 
+// Exponent-sum table: every primitive pair carries the id of its exponent
+// sum p among the distinct sums of the basis; entry (i, j) holds the
+// quantities of a primitive quartet that depend only on p_i and q_j:
+// {(p+q)^(-1/2), 1/(p+q), q/(p+q) = rho/p, p/(p+q) = rho/q}.
+struct __align__(32) ExpPair64 {
+  double rs, inv, rp, rq;
+};
+struct __align__(16) ExpPair32 {
+  float rs, inv, rp, rq;
+};
+
 // One launch of one class: rows are bra pairs; row r covers the kets
-// ket_list[row_beg[r] .. row_beg[r] + row_cnt[r]); each warp takes one row
-// and 32 consecutive kets; row_warp_off is the exclusive prefix sum of
-// ceil(row_cnt / 32).  Schwarz mode: bra_list holds nrows pairs, one per thread.
+// ket_list[row_beg[r] .. row_beg[r] + row_cnt[r]); each warp takes one row,
+// 32 consecutive kets and one of row_slices[r] slices of the bra primitive
+// pairs (the recurrences after the primitive loop are linear, so every slice
+// digests its partial sums on its own); row_warp_off is the exclusive prefix
+// sum of ceil(row_cnt / 32) * row_slices.  Schwarz mode: bra_list holds
+// nrows pairs, one per thread.
 struct ClassLaunch {
   const int* bra_list;
   const int* ket_list;
   const int* row_beg;
   const int* row_cnt;
+  const int* row_slices;
   const long long* row_warp_off;
   int nrows;
   long long nwarps;
@@ -67,13 +87,16 @@ struct EriArgs {
   const PrimPair64* prim64;
   const PrimPair32* prim32;
   const double* boys64;   // [kBoysMaxM+1][kBoysPts][kBoysTerms]
-  const double* exp64;    // [kBoysPts]
   const float* boys32;    // [kBoysMaxM+1][kBoysPts][kBoysTerms]
+  const ExpPair64* xp64;  // [nxp][nxp]
+  const ExpPair32* xp32;
+  int nxp;
   const double* D;        // density, nbf x nbf row-major (textbook sign convention)
   const float* D32;       // float copy for the FP32 digestion
   double* M;              // accumulator: G = M + M^T
   double* tensor;         // MODE_TENSOR output, nbf^4
   float* schwarz;         // MODE_SCHWARZ output per pair
+  double* grad;           // MODE_GRAD output, 3 * natom
   int nbf;
 };
 
@@ -81,29 +104,33 @@ struct EriArgs {
 // Scalar helpers
 // ---------------------------------------------------------------------------
 
+// Float approximation of a non-negative double from its high word with
+// integer operations only (relative error < 2^-20), so that table indexing
+// and seeds cost no FP64-pipe conversion.  Values below 2^-126 give 0.
+__device__ __forceinline__ float approx_float(double x) {
+  const int hi = __double2hiint(x);
+  const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
+  const int bits = (e << 23) | ((hi & 0xfffff) << 3);
+  return e <= 0 ? 0.0f : (e >= 255 ? __int_as_float(0x7f800000) : __int_as_float(bits));
+}
+
 // 1/sqrt(x) in double: single-precision hardware estimate refined by one
 // Halley-type step y' = y (1 + e/2 + 3e^2/8), e = 1 - x y^2 (the third-order
 // Householder iteration for x^{-1/2}; see Muller et al., Handbook of
-// Floating-Point Arithmetic, ch. 5).  Seed error ~1e-7 -> ~1e-21 + rounding.
+// Floating-Point Arithmetic, ch. 5).  Seed error ~1e-7 -> ~1e-20 + rounding.
 __device__ __forceinline__ double rsqrt_fp64(double x) {
-  double y = (double)rsqrtf((float)x);
+  double y = (double)rsqrtf(approx_float(x));
   double t = x * y;
   double e = fma(-t, y, 1.0);
   double c = fma(e, 0.375, 0.5);
+  // seed error ~2^-20 (approx_float) -> cubic step leaves ~1e-18
   return fma(y * e, c, y);
 }
-
-template <typename R>
-__device__ __forceinline__ R rsqrt_r(R x);
-template <>
-__device__ __forceinline__ double rsqrt_r<double>(double x) { return rsqrt_fp64(x); }
-template <>
-__device__ __forceinline__ float rsqrt_r<float>(float x) { return rsqrtf(x); }
 
 // Component normalisation relative to the x^l component: the reference
 // normalises every Cartesian component on its own (primitives.rs:19-27), so
 // factor = sqrt( ((2l)!/l!) / prod_axis (2n)!/n! ).  Order: reference order.
-__device__ __forceinline__ double comp_factor(int l, int c) {
+__host__ __device__ __forceinline__ double comp_factor(int l, int c) {
   if (l == 2) return (c == 1 || c == 3 || c == 4) ? 1.7320508075688772 : 1.0;
   if (l == 3) {
     // (003)(012)(021)(030)(102)(111)(120)(201)(210)(300)
@@ -120,51 +147,45 @@ __device__ __forceinline__ double comp_factor(int l, int c) {
 // ---------------------------------------------------------------------------
 // Boys function F_0..F_L at T, each multiplied by pref.
 // ---------------------------------------------------------------------------
+__device__ __forceinline__ double boys_taylor_row(const double* __restrict__ row, double d, double* ex) {
+  const double2* r2 = reinterpret_cast<const double2*>(row);
+  const double2 c01 = __ldg(r2), c23 = __ldg(r2 + 1), c45 = __ldg(r2 + 2), c6e = __ldg(r2 + 3);
+  double f = fma(c6e.x, d, c45.y);
+  f = fma(f, d, c45.x);
+  f = fma(f, d, c23.y);
+  f = fma(f, d, c23.x);
+  f = fma(f, d, c01.y);
+  f = fma(f, d, c01.x);
+  *ex = c6e.y;
+  return f;
+}
+
 template <int L>
-__device__ __forceinline__ void boys_scaled(double T, double pref, const double* __restrict__ tab,
-                                            const double* __restrict__ etab, double* F) {
+__device__ __forceinline__ void boys_scaled(double T, double pref, const double* __restrict__ tab, double* F) {
   if (T < kBoysTmax) {
-    int i = __float2int_rn((float)T * 16.0f);
+    int i = __float2int_rn(approx_float(T) * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
-    const double d = T - (double)i * 0.0625;
+    const double d = fma((double)i, -1.0 / kBoysPerUnit, T);
+    double ex;
     if (L <= 1) {
 #pragma unroll
-      for (int m = 0; m <= L; ++m) {
-        const double2* row = reinterpret_cast<const double2*>(tab + ((size_t)m * kBoysPts + i) * kBoysTerms);
-        double2 c01 = __ldg(row), c23 = __ldg(row + 1), c45 = __ldg(row + 2), c67 = __ldg(row + 3);
-        double f = fma(c67.y, d, c67.x);
-        f = fma(f, d, c45.y);
-        f = fma(f, d, c45.x);
-        f = fma(f, d, c23.y);
-        f = fma(f, d, c23.x);
-        f = fma(f, d, c01.y);
-        f = fma(f, d, c01.x);
-        F[m] = f * pref;
-      }
+      for (int m = 0; m <= L; ++m)
+        F[m] = boys_taylor_row(tab + ((size_t)m * kBoysPts + i) * kBoysTerms, d, &ex) * pref;
     } else {
-      const double2* row = reinterpret_cast<const double2*>(tab + ((size_t)L * kBoysPts + i) * kBoysTerms);
-      double2 c01 = __ldg(row), c23 = __ldg(row + 1), c45 = __ldg(row + 2), c67 = __ldg(row + 3);
-      double f = fma(c67.y, d, c67.x);
-      f = fma(f, d, c45.y);
-      f = fma(f, d, c45.x);
-      f = fma(f, d, c23.y);
-      f = fma(f, d, c23.x);
-      f = fma(f, d, c01.y);
-      f = fma(f, d, c01.x);
-      // exp(-T) = exp(-T_i) * exp(-d), Taylor of exp(-d) to d^7
+      const double f = boys_taylor_row(tab + ((size_t)L * kBoysPts + i) * kBoysTerms, d, &ex);
+      // e^{-T} = e^{-T_i} e^{-d}
       const double nd = -d;
-      double ex = fma(nd, 1.0 / 5040.0, 1.0 / 720.0);
-      ex = fma(ex, nd, 1.0 / 120.0);
-      ex = fma(ex, nd, 1.0 / 24.0);
-      ex = fma(ex, nd, 1.0 / 6.0);
-      ex = fma(ex, nd, 0.5);
-      ex = fma(ex, nd, 1.0);
-      ex = fma(ex, nd, 1.0);
-      ex *= __ldg(etab + i);
+      double e = fma(nd, 1.0 / 720.0, 1.0 / 120.0);
+      e = fma(e, nd, 1.0 / 24.0);
+      e = fma(e, nd, 1.0 / 6.0);
+      e = fma(e, nd, 0.5);
+      e = fma(e, nd, 1.0);
+      e = fma(e, nd, 1.0);
+      e *= ex;
       const double t2 = T + T;
       F[L] = f;
 #pragma unroll
-      for (int m = L; m > 0; --m) F[m - 1] = fma(t2, F[m], ex) * (1.0 / (2 * m - 1));
+      for (int m = L; m > 0; --m) F[m - 1] = fma(t2, F[m], e) * (1.0 / (2 * m - 1));
 #pragma unroll
       for (int m = 0; m <= L; ++m) F[m] *= pref;
     }
@@ -182,18 +203,15 @@ __device__ __forceinline__ void boys_scaled(double T, double pref, const double*
 }
 
 template <int L>
-__device__ __forceinline__ void boys_scaled(float T, float pref, const float* __restrict__ tab, const double*,
-                                            float* F) {
+__device__ __forceinline__ void boys_scaled(float T, float pref, const float* __restrict__ tab, float* F) {
   if (T < kBoysTmaxF) {
-    int i = __float2int_rn(T * 16.0f);
+    int i = __float2int_rn(T * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
-    const float d = T - (float)i * 0.0625f;
-    const float4* row = reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysPts + i) * kBoysTerms);
-    float4 c0 = __ldg(row), c1 = __ldg(row + 1);
-    float f = fmaf(c1.x, d, c0.w);
-    f = fmaf(f, d, c0.z);
-    f = fmaf(f, d, c0.y);
-    f = fmaf(f, d, c0.x);
+    const float d = fmaf((float)i, -1.0f / kBoysPerUnit, T);
+    const float4 c = __ldg(reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysPts + i) * kBoysTerms));
+    float f = fmaf(c.w, d, c.z);
+    f = fmaf(f, d, c.y);
+    f = fmaf(f, d, c.x);
     F[L] = f;
     if (L > 0) {
       const float ex = __expf(-T);

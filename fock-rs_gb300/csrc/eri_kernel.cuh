@@ -18,11 +18,18 @@
 // which gives G = J - K/2 = M + M^T for a symmetric density.
 #pragma once
 #include "common.cuh"
-#include "gen/eri_classes.cuh"
+// the class struct (generated gen/cls_*.cuh) is included before this header
 
 namespace fockgb {
 
 constexpr int kEriThreads = 128;
+
+// unroll factor of the ket primitive loop (independent iterations interleave:
+// instruction-level parallelism for the long FP64 dependency chains)
+#ifndef FOCK_KET_UNROLL
+#define FOCK_KET_UNROLL 2
+#endif
+constexpr int kKetUnroll = FOCK_KET_UNROLL;
 
 template <typename R>
 struct PrimLoad;
@@ -30,22 +37,38 @@ struct PrimLoad;
 template <>
 struct PrimLoad<double> {
   double p, o2p, K, P[3], PA[3];
+  int eid;
   __device__ __forceinline__ void load(const EriArgs& a, int idx) {
     const double2* v = a.prim64[idx].v;
     double2 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2), v3 = __ldg(v + 3), v4 = __ldg(v + 4);
     p = v0.x; o2p = v0.y; K = v1.x; P[0] = v1.y; P[1] = v2.x; P[2] = v2.y;
     PA[0] = v3.x; PA[1] = v3.y; PA[2] = v4.x;
+    eid = (int)__double_as_longlong(v4.y);
+  }
+  // (p+q)^(-1/2), 1/(p+q), rho/p, rho/q for this bra exponent sum and eid_k
+  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, double& rs, double& inv, double& rp,
+                                       double& rq) const {
+    const double2* x = reinterpret_cast<const double2*>(a.xp64 + (size_t)eid * a.nxp + eid_k);
+    const double2 x0 = __ldg(x), x1 = __ldg(x + 1);
+    rs = x0.x; inv = x0.y; rp = x1.x; rq = x1.y;
   }
 };
 
 template <>
 struct PrimLoad<float> {
   float p, o2p, K, P[3], PA[3];
+  int eid;
   __device__ __forceinline__ void load(const EriArgs& a, int idx) {
     const float4* v = a.prim32[idx].v;
     float4 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2);
     p = v0.x; o2p = v0.y; K = v0.z; P[0] = v0.w; P[1] = v1.x; P[2] = v1.y;
     PA[0] = v1.z; PA[1] = v1.w; PA[2] = v2.x;
+    eid = __float_as_int(v2.y);
+  }
+  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, float& rs, float& inv, float& rp,
+                                       float& rq) const {
+    const float4 x = __ldg(reinterpret_cast<const float4*>(a.xp32 + (size_t)eid * a.nxp + eid_k));
+    rs = x.x; inv = x.y; rp = x.z; rq = x.w;
   }
 };
 
@@ -80,6 +103,7 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   const int lane = threadIdx.x & 31;
   int bra, ket;
   bool active;
+  int slice = 0, nslice = 1;
   if (MODE == MODE_SCHWARZ) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     active = t < cl.nrows;
@@ -92,7 +116,10 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
       const int mid = (lo + hi + 1) >> 1;
       if (__ldg(cl.row_warp_off + mid) <= gw) lo = mid; else hi = mid - 1;
     }
-    const int k = (int)(gw - __ldg(cl.row_warp_off + lo)) * 32 + lane;
+    const int w = (int)(gw - __ldg(cl.row_warp_off + lo));
+    nslice = cl.row_slices ? __ldg(cl.row_slices + lo) : 1;
+    slice = w % nslice;
+    const int k = (w / nslice) * 32 + lane;
     const int cnt = __ldg(cl.row_cnt + lo);
     active = k < cnt;
     bra = __ldg(cl.bra_list + lo);
@@ -100,7 +127,9 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   }
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
-  const int nbp = Pb.nprim;
+  // this warp's slice of the bra primitive pairs
+  const int ib0 = (int)(((long long)slice * Pb.nprim) / nslice);
+  const int ib1 = (int)(((long long)(slice + 1) * Pb.nprim) / nslice);
   const int nkp = active ? Pk.nprim : 0;
   const int bp0 = Pb.prim_off, kp0 = Pk.prim_off;
 
@@ -109,23 +138,21 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   for (int i = 0; i < NE * NF; ++i) acc[i] = R(0);
 
   const R* btab = boys_table<R>(a);
-  for (int ib = 0; ib < nbp; ++ib) {
+  for (int ib = ib0; ib < ib1; ++ib) {
     PrimLoad<R> bp;
     bp.load(a, bp0 + ib);
+#pragma unroll kKetUnroll
     for (int ik = 0; ik < nkp; ++ik) {
       PrimLoad<R> kp;
       kp.load(a, kp0 + ik);
-      const R s = bp.p + kp.p;
-      const R rs = rsqrt_r<R>(s);
-      const R inv = rs * rs;
-      const R rp = kp.p * inv;   // rho / p
-      const R rq = bp.p * inv;   // rho / q
+      R rs, inv, rp, rq;  // (p+q)^(-1/2), 1/(p+q), rho/p, rho/q from the exponent-sum table
+      bp.exps(a, kp.eid, rs, inv, rp, rq);
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const R r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
       const R T = bp.p * rp * r2;  // rho |PQ|^2, rho = p q / (p + q)
       const R pref = bp.K * kp.K * rs;
       R F[L + 1];
-      boys_scaled<L>(T, pref, btab, a.exp64, F);
+      boys_scaled<L>(T, pref, btab, F);
       const R WP[3] = {-rp * PQ[0], -rp * PQ[1], -rp * PQ[2]};
       const R WQ[3] = {rq * PQ[0], rq * PQ[1], rq * PQ[2]};
       const R o2pq = R(0.5) * inv;
@@ -273,8 +300,129 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   }
 }
 
+// Nuclear gradient of the two-electron energy, fused: derivative integrals
+// (a+1_i b|cd), (a-1_i b|cd), ... are built per contracted quartet from
+// weighted primitive accumulators (2 alpha, 2 beta, 2 gamma, 1) and
+// contracted at once with the RHF two-particle density
+//   Gam_ijkl = D_ij D_kl - (D_ik D_jl + D_il D_jk) / 4,
+// E_2e = sum over unique quartets 4 s Gam (ij|kl), so the gradient takes
+// 4 s Gam (ij|kl)^x.  The D-centre derivative follows from translational
+// invariance: d_D = -(d_A + d_B + d_C).  Same work mapping as MODE_JK.
+template <class C>
+__global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch cl, const EriArgs a) {
+  constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, LG = C::LG;
+  const int lane = threadIdx.x & 31;
+  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (gw >= cl.nwarps) return;
+  int lo = 0, hi = cl.nrows - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(cl.row_warp_off + mid) <= gw) lo = mid; else hi = mid - 1;
+  }
+  const int w = (int)(gw - __ldg(cl.row_warp_off + lo));
+  const int nslice = cl.row_slices ? __ldg(cl.row_slices + lo) : 1;
+  const int slice = w % nslice;
+  const int k = (w / nslice) * 32 + lane;
+  const bool active = k < __ldg(cl.row_cnt + lo);
+  const int bra = __ldg(cl.bra_list + lo);
+  const int ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + (active ? k : 0));
+  const PairInfo& Pb = a.pairs[bra];
+  const PairInfo& Pk = a.pairs[ket];
+  const int ib0 = (int)(((long long)slice * Pb.nprim) / nslice);
+  const int ib1 = (int)(((long long)(slice + 1) * Pb.nprim) / nslice);
+  const int nkp = active ? Pk.nprim : 0;
+
+  double acc0[C::NACC0], accA[C::NACCA], accB[C::NACCB], accC[C::NACCC];
+#pragma unroll
+  for (int i = 0; i < C::NACC0; ++i) acc0[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < C::NACCA; ++i) accA[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < C::NACCB; ++i) accB[i] = 0.0;
+#pragma unroll
+  for (int i = 0; i < C::NACCC; ++i) accC[i] = 0.0;
+
+  for (int ib = ib0; ib < ib1; ++ib) {
+    PrimLoad<double> bp;
+    bp.load(a, Pb.prim_off + ib);
+    const double alpha = __ldg(&a.prim64[Pb.prim_off + ib].v[5].x);
+    const double wa = 2.0 * alpha, wb = 2.0 * (bp.p - alpha);
+    for (int ik = 0; ik < nkp; ++ik) {
+      PrimLoad<double> kp;
+      kp.load(a, Pk.prim_off + ik);
+      const double wc = 2.0 * __ldg(&a.prim64[Pk.prim_off + ik].v[5].x);
+      double rs, inv, rp, rq;
+      bp.exps(a, kp.eid, rs, inv, rp, rq);
+      const double PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
+      const double r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
+      const double T = bp.p * rp * r2;
+      const double pref = bp.K * kp.K * rs;
+      double F[LG + 1];
+      boys_scaled<LG>(T, pref, a.boys64, F);
+      const double WP[3] = {-rp * PQ[0], -rp * PQ[1], -rp * PQ[2]};
+      const double WQ[3] = {rq * PQ[0], rq * PQ[1], rq * PQ[2]};
+      C::template vrr_grad<double>(F, bp.PA, WP, kp.PA, WQ, bp.o2p, kp.o2p, 0.5 * inv, rp, rq, wa, wb, wc, acc0, accA,
+                                   accB, accC);
+    }
+  }
+  double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
+  if (active) {
+    const int fa = Pb.fa, fb = Pb.fb, fc = Pk.fa, fd = Pk.fb;
+    double gam[NA * NB * NC * ND];
+#pragma unroll
+    for (int ia = 0; ia < NA; ++ia)
+#pragma unroll
+      for (int ib = 0; ib < NB; ++ib)
+#pragma unroll
+        for (int ic = 0; ic < NC; ++ic)
+#pragma unroll
+          for (int id = 0; id < ND; ++id) {
+            const double dab = dens<double>(a, fa + ia, fb + ib), dcd = dens<double>(a, fc + ic, fd + id);
+            const double dac = dens<double>(a, fa + ia, fc + ic), dbd = dens<double>(a, fb + ib, fd + id);
+            const double dad = dens<double>(a, fa + ia, fd + id), dbc = dens<double>(a, fb + ib, fc + ic);
+            gam[((ia * NB + ib) * NC + ic) * ND + id] =
+                (dab * dcd - 0.25 * (dac * dbd + dad * dbc)) *
+                (comp_factor(C::LA, ia) * comp_factor(C::LB, ib) * comp_factor(C::LC, ic) * comp_factor(C::LD, id));
+          }
+    double AB[3], CD[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { AB[i] = Pb.AB[i]; CD[i] = Pk.AB[i]; }
+    double g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    C::template hrr_grad<double>(acc0, accA, accB, accC, AB, CD, gam, g);
+    const double sdeg = 4.0 * (Pb.sa == Pb.sb ? 0.5 : 1.0) * (Pk.sa == Pk.sb ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) { gA[i] = sdeg * g[i]; gB[i] = sdeg * g[3 + i]; gC[i] = sdeg * g[6 + i]; }
+  }
+  // bra centres are uniform across the warp: reduce first
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const double sa = warp_sum(gA[i]), sb = warp_sum(gB[i]);
+    if (lane == 0) {
+      if (sa != 0.0) atomicAdd(a.grad + 3 * Pb.atom_a + i, sa);
+      if (sb != 0.0) atomicAdd(a.grad + 3 * Pb.atom_b + i, sb);
+    }
+  }
+  if (!active) return;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    atomicAdd(a.grad + 3 * Pk.atom_a + i, gC[i]);
+    atomicAdd(a.grad + 3 * Pk.atom_b + i, -(gA[i] + gB[i] + gC[i]));
+  }
+}
+
 template <class C>
 cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if (mode == MODE_GRAD) {
+    if constexpr (C::HAS_GRAD) {
+      if (cl.nwarps <= 0) return cudaSuccess;
+      const long long blocks = (cl.nwarps * 32 + kEriThreads - 1) / kEriThreads;
+      if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+      eri_grad_kernel<C><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+      return cudaGetLastError();
+    } else {
+      return cudaErrorNotSupported;
+    }
+  }
   if (mode == MODE_SCHWARZ) {
     if (cl.nrows <= 0) return cudaSuccess;
     if constexpr (C::LA == C::LC && C::LB == C::LD) {

@@ -35,6 +35,7 @@ using namespace fockgb;
 namespace {
 
 constexpr int kMaxL = 2;
+constexpr int kForkStreams = 8;
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
 
 inline int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
@@ -47,9 +48,9 @@ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 // (positive terms, no cancellation) for the top order in long double, then
 // the stable downward recursion F_{n-1} = (2T F_n + e^{-T}) / (2n-1).
 // ---------------------------------------------------------------------------
-constexpr int kTabOrders = kBoysMaxM + kBoysTerms;  // F_0 .. F_{M+7}
+constexpr int kTabOrders = kBoysMaxM + kBoysTaylor;  // F_0 .. F_{M+6}
 std::once_flag g_tab_once;
-std::vector<double> g_boys64, g_exp64, g_ref_lut;
+std::vector<double> g_boys64, g_ref_lut;
 std::vector<float> g_boys32;
 
 long double boys_series_ld(int n, long double T) {
@@ -65,7 +66,7 @@ long double boys_series_ld(int n, long double T) {
 void build_tables() {
   std::vector<long double> F((size_t)kBoysPts * (kTabOrders + 1));
   for (int i = 0; i < kBoysPts; ++i) {
-    const long double T = (long double)i / 16.0L;
+    const long double T = (long double)i / (long double)kBoysPerUnit;
     const long double e = expl(-T);
     long double f = boys_series_ld(kTabOrders, T);
     F[(size_t)i * (kTabOrders + 1) + kTabOrders] = f;
@@ -76,20 +77,21 @@ void build_tables() {
   }
   g_boys64.assign((size_t)(kBoysMaxM + 1) * kBoysPts * kBoysTerms, 0.0);
   g_boys32.assign(g_boys64.size(), 0.0f);
-  g_exp64.resize(kBoysPts);
   for (int M = 0; M <= kBoysMaxM; ++M)
     for (int i = 0; i < kBoysPts; ++i) {
       long double fact = 1.0L;
-      for (int k = 0; k < kBoysTerms; ++k) {
+      const size_t row = ((size_t)M * kBoysPts + i) * kBoysTerms;
+      for (int k = 0; k < kBoysTaylor; ++k) {
         if (k > 0) fact *= k;
         long double c = F[(size_t)i * (kTabOrders + 1) + M + k] / fact;
         if (k & 1) c = -c;
-        const size_t idx = ((size_t)M * kBoysPts + i) * kBoysTerms + k;
-        g_boys64[idx] = (double)c;
-        g_boys32[idx] = (float)c;
+        g_boys64[row + k] = (double)c;
+        g_boys32[row + k] = (float)c;
       }
+      const long double ex = expl(-(long double)i / (long double)kBoysPerUnit);
+      g_boys64[row + kBoysTaylor] = (double)ex;
+      g_boys32[row + kBoysTaylor] = (float)ex;
     }
-  for (int i = 0; i < kBoysPts; ++i) g_exp64[i] = (double)expl(-(long double)i / 16.0L);
   // reference LUT: F_10(0.15 k), k < 200 (boys/src/lut.rs values, regenerated)
   g_ref_lut.resize(200);
   for (int k = 0; k < 200; ++k) g_ref_lut[k] = (double)boys_series_ld(10, (long double)((double)k * 0.15));
@@ -159,7 +161,10 @@ struct fock_ctx {
   PairInfo* d_pairs = nullptr;
   PrimPair64* d_prim64 = nullptr;
   PrimPair32* d_prim32 = nullptr;
-  double *d_boys64 = nullptr, *d_exp64 = nullptr, *d_ref_lut = nullptr;
+  double *d_boys64 = nullptr, *d_ref_lut = nullptr;
+  ExpPair64* d_xp64 = nullptr;
+  ExpPair32* d_xp32 = nullptr;
+  int nxp = 0;
   float* d_boys32 = nullptr;
   float* d_schwarz = nullptr;
   std::vector<float> Q;
@@ -174,11 +179,19 @@ struct fock_ctx {
   // MD basis (one-electron, refcompat tensor)
   MdFunc* d_mdfuncs = nullptr;
   double *d_mdexps = nullptr, *d_mdcoefs = nullptr, *d_atoms4 = nullptr;
+  int* d_func_atom = nullptr;
   // dense tensor (refcompat SCF)
   double* d_tensor = nullptr;
   // SCF library handles
   cublasHandle_t blas = nullptr;
   cusolverDnHandle_t solver = nullptr;
+  // captured Fock build
+  cudaStream_t cap_stream = nullptr;
+  cudaStream_t side[kForkStreams] = {};
+  cudaEvent_t fork_ev = nullptr;
+  cudaEvent_t join_ev[kForkStreams] = {};
+  cudaGraphExec_t jk_exec = nullptr;
+  int jk_kernels = 0;
 };
 
 namespace {
@@ -189,13 +202,16 @@ EriArgs eri_args(fock_ctx* c) {
   a.prim64 = c->d_prim64;
   a.prim32 = c->d_prim32;
   a.boys64 = c->d_boys64;
-  a.exp64 = c->d_exp64;
   a.boys32 = c->d_boys32;
+  a.xp64 = c->d_xp64;
+  a.xp32 = c->d_xp32;
+  a.nxp = c->nxp;
   a.D = c->d_D;
   a.D32 = c->d_D32;
   a.M = c->d_M;
   a.tensor = nullptr;
   a.schwarz = c->d_schwarz;
+  a.grad = nullptr;
   a.nbf = c->nbf;
   return a;
 }
@@ -212,18 +228,26 @@ MdBasis md_basis(fock_ctx* c) {
 MdTables md_tables(fock_ctx* c) {
   MdTables t;
   t.boys64 = c->d_boys64;
-  t.exp64 = c->d_exp64;
   t.ref_lut = c->d_ref_lut;
   return t;
 }
 
-// Per-primitive-quartet flops outside the generated VRR: pair setup
-// (s, rsqrt, 1/s, rho/p, rho/q, PQ, |PQ|^2, T, prefactor, WP, WQ, 1/(2(p+q)))
-// and the Boys evaluation of kernel common.cuh (FMA = 2 flops).
-long long setup_flops(int L) {
-  long long f = 32;
-  if (L <= 1) f += (L + 1) * 15 + 2;
-  else f += 14 + 15 + 2 + 3LL * L + (L + 1);
+// Per-primitive-quartet flops outside the generated VRR (FMA = 2 flops), as
+// the kernel evaluates them: PQ (3), |PQ|^2 (5), T = p (rho/p) |PQ|^2 (2),
+// prefactor (2), WP and WQ when the bra / ket carries angular momentum (3
+// each), 1/(2(p+q)) when both do, the table offset d (2) and the Boys
+// function: per order a 7-term Horner (12) and the prefactor (1) for L <= 1;
+// otherwise one Horner (12), e^{-T} (11), 2T (1), the downward recursion
+// (3 per order) and the prefactors (L + 1).  The exponent-sum quantities
+// come from a table (no flops).
+long long setup_flops(int la, int lb, int lc, int ld) {
+  const int L = la + lb + lc + ld;
+  long long f = 12 + 2;
+  if (la + lb > 0) f += 3;
+  if (lc + ld > 0) f += 3;
+  if (la + lb > 0 && lc + ld > 0) f += 1;
+  if (L <= 1) f += (L + 1) * 13;
+  else f += 12 + 11 + 1 + 3LL * L + (L + 1);
   return f;
 }
 
@@ -231,6 +255,7 @@ int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
 
 // Build the quartet plans from the Schwarz factors.
 int build_plan(fock_ctx* c, bool for_tensor) {
+  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
   dfree(c->d_plan_int);
   dfree(c->d_plan_ll);
   c->plans.clear();
@@ -249,7 +274,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   }
   std::vector<int> ints;
   std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, off; };
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
   std::vector<Pending> pend;
   fock_stats st{};
   st.shell_pairs = npairs;
@@ -352,14 +377,21 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           ints.insert(ints.end(), rbeg.begin(), rbeg.end());
           P.cnt = ints.size();
           ints.insert(ints.end(), rcnt.begin(), rcnt.end());
+          // bra primitive slices per row: at most pps primitive pairs per warp
+          P.sl = ints.size();
+          const int pps = for_tensor ? (1 << 30)
+                          : std::max(1, P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
+          std::vector<int> rsl(rbra.size());
+          for (size_t r = 0; r < rbra.size(); ++r) rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + pps - 1) / pps);
+          ints.insert(ints.end(), rsl.begin(), rsl.end());
           P.off = lls.size();
           long long acc = 0;
-          for (int cnt : rcnt) { lls.push_back(acc); acc += (cnt + 31) / 32; }
+          for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)((rcnt[r] + 31) / 32) * rsl[r]; }
           lls.push_back(acc);
           P.p.cl.nrows = (int)rbra.size();
           P.p.cl.nwarps = acc;
           pend.push_back(P);
-          const long long flops = pq * ((long long)vrr + setup_flops(L)) + q * ((long long)hrr + 12LL * neri);
+          const long long flops = pq * ((long long)vrr + setup_flops(la, lb, lc, ld)) + q * ((long long)hrr + 12LL * neri);
           pend.back().p.flops = flops;
           if (P.p.prec == PREC_FP32) {
             st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
@@ -380,6 +412,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.ket_list = c->d_plan_int + P.ket;
     P.p.cl.row_beg = c->d_plan_int + P.beg;
     P.p.cl.row_cnt = c->d_plan_int + P.cnt;
+    P.p.cl.row_slices = c->d_plan_int + P.sl;
     P.p.cl.row_warp_off = c->d_plan_ll + P.off;
     c->plans.push_back(P.p);
   }
@@ -474,6 +507,8 @@ void fock_options_default(fock_options* o) {
   o->diis_start = 5;
   o->energy_mode = 0;
   o->final_fp64 = 1;
+  o->prims_per_slice = 1;
+  o->prims_per_slice_fp32 = 4;
   o->device = 0;
 }
 
@@ -515,13 +550,20 @@ void fock_ctx_destroy(fock_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
-  dfree(c->d_boys64); dfree(c->d_exp64); dfree(c->d_ref_lut); dfree(c->d_boys32);
+  dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64); dfree(c->d_xp32);
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
   dfree(c->d_plan_int); dfree(c->d_plan_ll);
-  dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4);
+  dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
   dfree(c->d_tensor);
   if (c->blas) cublasDestroy(c->blas);
   if (c->solver) cusolverDnDestroy(c->solver);
+  if (c->jk_exec) cudaGraphExecDestroy(c->jk_exec);
+  for (int k = 0; k < kForkStreams; ++k) {
+    if (c->side[k]) cudaStreamDestroy(c->side[k]);
+    if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
 }
@@ -573,6 +615,13 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
   auto fail = [&](int code) { fock_ctx_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FOCK_ERR_CUDA);
   c->stream = c->own_stream;
+  if (cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    return fail(FOCK_ERR_CUDA);
+  for (int k = 0; k < kForkStreams; ++k)
+    if (cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return fail(FOCK_ERR_CUDA);
 
   // ---- shell pairs and primitive pairs ----
   std::vector<PrimPair64> p64;
@@ -586,6 +635,7 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       PairInfo P{};
       P.prim_off = (int)p64.size();
       P.fa = A.f0; P.fb = B.f0; P.sa = a; P.sb = b;
+      P.atom_a = A.atom; P.atom_b = B.atom;
       P.cls = pair_class(A.l, B.l);
       for (int k = 0; k < 3; ++k) P.AB[k] = A.c[k] - B.c[k];
       const double ab2 = P.AB[0] * P.AB[0] + P.AB[1] * P.AB[1] + P.AB[2] * P.AB[2];
@@ -605,6 +655,7 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
           q.v[2] = make_double2(Pc[1], Pc[2]);
           q.v[3] = make_double2(PA[0], PA[1]);
           q.v[4] = make_double2(PA[2], 0.0);
+          q.v[5] = make_double2(ea, 0.0);
           p64.push_back(q);
           PrimPair32 r;
           r.v[0] = make_float4((float)p, (float)(0.5 / p), (float)K, (float)Pc[0]);
@@ -616,6 +667,36 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       c->hpairs.push_back(P);
     }
   c->nprim_pairs = (long long)p64.size();
+  // distinct exponent sums -> ids, and the (p, q) table of the quantities that
+  // depend only on the two sums (computed here in extended precision)
+  std::vector<double> psum;
+  for (const PrimPair64& q : p64) psum.push_back(q.v[0].x);
+  std::sort(psum.begin(), psum.end());
+  psum.erase(std::unique(psum.begin(), psum.end()), psum.end());
+  c->nxp = (int)psum.size();
+  if (c->nxp > 8192) return fail(FOCK_ERR_TOO_LARGE);
+  for (size_t k = 0; k < p64.size(); ++k) {
+    const long long id = std::lower_bound(psum.begin(), psum.end(), p64[k].v[0].x) - psum.begin();
+    double idd;
+    std::memcpy(&idd, &id, sizeof(idd));
+    p64[k].v[4].y = idd;
+    int idi = (int)id;
+    float idf;
+    std::memcpy(&idf, &idi, sizeof(idf));
+    p32[k].v[2].y = idf;
+  }
+  std::vector<ExpPair64> xp64((size_t)c->nxp * c->nxp);
+  std::vector<ExpPair32> xp32(xp64.size());
+  for (int i = 0; i < c->nxp; ++i)
+    for (int j = 0; j < c->nxp; ++j) {
+      const long double p = psum[i], q = psum[j], s = p + q;
+      ExpPair64& e = xp64[(size_t)i * c->nxp + j];
+      e.rs = (double)(1.0L / sqrtl(s));
+      e.inv = (double)(1.0L / s);
+      e.rp = (double)(q / s);
+      e.rq = (double)(p / s);
+      xp32[(size_t)i * c->nxp + j] = ExpPair32{(float)e.rs, (float)e.inv, (float)e.rp, (float)e.rq};
+    }
   const int npairs = (int)c->hpairs.size();
   const size_t nn = (size_t)c->nbf * c->nbf;
   if ((rc = map_cuda(dalloc(&c->d_pairs, npairs))) ||
@@ -623,7 +704,8 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       (rc = map_cuda(dalloc(&c->d_prim32, p32.size()))) ||
       (rc = map_cuda(dalloc(&c->d_boys64, g_boys64.size()))) ||
       (rc = map_cuda(dalloc(&c->d_boys32, g_boys32.size()))) ||
-      (rc = map_cuda(dalloc(&c->d_exp64, g_exp64.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_xp64, xp64.size()))) ||
+      (rc = map_cuda(dalloc(&c->d_xp32, xp32.size()))) ||
       (rc = map_cuda(dalloc(&c->d_ref_lut, g_ref_lut.size()))) ||
       (rc = map_cuda(dalloc(&c->d_schwarz, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_D, nn))) || (rc = map_cuda(dalloc(&c->d_M, nn))) ||
@@ -634,7 +716,8 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       (rc = map_cuda(cudaMemcpy(c->d_prim32, p32.data(), p32.size() * sizeof(PrimPair32), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_boys64, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_boys32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_exp64, g_exp64.data(), g_exp64.size() * 8, cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_xp64, xp64.data(), xp64.size() * sizeof(ExpPair64), cudaMemcpyHostToDevice))) ||
+      (rc = map_cuda(cudaMemcpy(c->d_xp32, xp32.data(), xp32.size() * sizeof(ExpPair32), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_ref_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice))))
     return fail(rc);
 
@@ -663,6 +746,12 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
     for (int a = 0; a < natom; ++a) {
       at4.push_back(atoms[a].x); at4.push_back(atoms[a].y); at4.push_back(atoms[a].z); at4.push_back((double)atoms[a].Z);
     }
+    std::vector<int> fatom;
+    for (const HostShell& h : c->shells)
+      for (int k = 0; k < ncart(h.l); ++k) fatom.push_back(h.atom);
+    if ((rc = map_cuda(dalloc(&c->d_func_atom, fatom.size()))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_func_atom, fatom.data(), fatom.size() * sizeof(int), cudaMemcpyHostToDevice))))
+      return fail(rc);
     if ((rc = map_cuda(dalloc(&c->d_mdfuncs, fl.size()))) || (rc = map_cuda(dalloc(&c->d_mdexps, ex.size()))) ||
         (rc = map_cuda(dalloc(&c->d_mdcoefs, cf.size()))) || (rc = map_cuda(dalloc(&c->d_atoms4, at4.size()))) ||
         (rc = map_cuda(cudaMemcpy(c->d_mdfuncs, fl.data(), fl.size() * sizeof(MdFunc), cudaMemcpyHostToDevice))) ||
@@ -687,26 +776,60 @@ int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
   return build_plan(c, false);
 }
 
-int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
-  if (!c || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
+// One Fock build from c->d_D into c->d_G as a CUDA graph: clear M, FP32 copy
+// of D, then the class launches forked over kForkStreams streams (largest
+// first, so that the small classes fill in behind them: a single small
+// molecule has too few quartets per class to fill 152 SMs on its own), join,
+// G = M + M^T.  Captured once per plan, replayed per build.
+static int capture_jk_graph(fock_ctx* c) {
+  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
   const int n = c->nbf;
   const size_t nn = (size_t)n * n;
-  CK(cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), c->stream));
+  cudaStream_t cs = c->cap_stream;
   EriArgs a = eri_args(c);
-  a.D = D_dev;
   bool need32 = false;
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
-  if (need32) {
-    CK(k_to_float(D_dev, c->d_D32, (int)nn, c->stream));
-    c->launches++;
+  std::vector<int> order(c->plans.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return c->plans[x].flops > c->plans[y].flops; });
+  const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
+  CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
+  int kernels = 0;
+  if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); kernels++; }
+  if (e == cudaSuccess) e = cudaEventRecord(c->fork_ev, cs);
+  for (int s = 0; s < nside && e == cudaSuccess; ++s) e = cudaStreamWaitEvent(c->side[s], c->fork_ev, 0);
+  for (size_t k = 0; k < order.size() && e == cudaSuccess; ++k) {
+    const Plan& p = c->plans[order[k]];
+    e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->side[k % nside]);
+    kernels++;
   }
-  for (const Plan& p : c->plans) {
-    cudaError_t e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->stream);
-    c->launches++;
-    CK(e);
+  for (int s = 0; s < nside && e == cudaSuccess; ++s) {
+    e = cudaEventRecord(c->join_ev[s], c->side[s]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, c->join_ev[s], 0);
   }
-  CK(k_symmetrize(c->d_M, G_dev, n, c->stream));
-  c->launches++;
+  if (e == cudaSuccess) { e = k_symmetrize(c->d_M, c->d_G, n, cs); kernels++; }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&c->jk_exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  CK(e);
+  c->jk_kernels = kernels;
+  return FOCK_OK;
+}
+
+int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
+  if (!c || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
+  const size_t nn = (size_t)c->nbf * c->nbf;
+  if (!c->jk_exec) {
+    int rc = capture_jk_graph(c);
+    if (rc != FOCK_OK) return rc;
+  }
+  if (D_dev != c->d_D) CK(cudaMemcpyAsync(c->d_D, D_dev, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+  CK(cudaGraphLaunch(c->jk_exec, c->stream));
+  c->launches += c->jk_kernels;
+  if (G_dev != c->d_G) CK(cudaMemcpyAsync(G_dev, c->d_G, nn * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
   return FOCK_OK;
 }
 
@@ -880,6 +1003,79 @@ int fock_one_electron(fock_ctx* c, double* S, double* T, double* V) {
   to_std(c, hT.data(), T);
   to_std(c, hV.data(), V);
   return FOCK_OK;
+}
+
+int fock_gradient(fock_ctx* c, const double* D, const double* W, double* grad) {
+  if (!c || !D || !W || !grad) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  if (c->opt.eri_mode != FOCK_ERI_EXACT) return FOCK_ERR_INVALID_ARG;
+  for (const HostShell& h : c->shells)
+    if (h.l > kGeneratedGradLmax) return FOCK_ERR_UNSUPPORTED_L;
+  const int n = c->nbf, na = c->natom;
+  const size_t nn = (size_t)n * n;
+  std::vector<double> Ds(nn), Ws(nn);
+  to_std(c, D, Ds.data());
+  to_std(c, W, Ws.data());
+  const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
+  const double tmix = c->opt.mixed_threshold;
+  int rc = FOCK_OK;
+  if (mixed && (rc = fock_set_precision(c, FOCK_PREC_FP64, tmix)) != FOCK_OK) return rc;
+  double *d_W = nullptr, *d_grad = nullptr;
+  cudaError_t e = dalloc(&d_W, nn);
+  if (e == cudaSuccess) e = dalloc(&d_grad, 3 * (size_t)na);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->d_D, Ds.data(), nn * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_W, Ws.data(), nn * 8, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_grad, 0, 3 * (size_t)na * 8, c->stream);
+  if (e == cudaSuccess) {
+    EriArgs a = eri_args(c);
+    a.D = c->d_D;
+    a.grad = d_grad;
+    for (const Plan& p : c->plans) {
+      e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_GRAD, PREC_FP64, c->stream);
+      c->launches++;
+      if (e != cudaSuccess) break;
+    }
+  }
+  if (e == cudaSuccess) {
+    e = md_one_electron_grad(md_basis(c), md_tables(c), c->d_atoms4, na, c->d_func_atom, 0, c->d_D, d_W, d_grad,
+                             c->stream);
+    c->launches++;
+  }
+  std::vector<double> g(3 * (size_t)na, 0.0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(g.data(), d_grad, g.size() * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_W);
+  cudaFree(d_grad);
+  if (mixed) fock_set_precision(c, FOCK_PREC_MIXED, tmix);
+  if (e == cudaErrorNotSupported) return FOCK_ERR_UNSUPPORTED_L;
+  CK(e);
+  // nuclear repulsion: d/dR_A sum_{A<B} Z_A Z_B / |R_A - R_B|
+  for (int A = 0; A < na; ++A)
+    for (int Bq = 0; Bq < na; ++Bq) {
+      if (A == Bq) continue;
+      const double d[3] = {c->atoms[A].x - c->atoms[Bq].x, c->atoms[A].y - c->atoms[Bq].y, c->atoms[A].z - c->atoms[Bq].z};
+      const double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+      const double f = -(double)c->atoms[A].Z * c->atoms[Bq].Z / (r2 * std::sqrt(r2));
+      for (int x = 0; x < 3; ++x) g[3 * A + x] += f * d[x];
+    }
+  std::memcpy(grad, g.data(), g.size() * 8);
+  return FOCK_OK;
+}
+
+int fock_energy_backward(fock_ctx* c, const fock_scf_result* r, double* grad) {
+  if (!c || !r || !grad || !r->density_matrix || !r->coefficient_matrix || !r->orbital_energies)
+    return FOCK_ERR_INVALID_ARG;
+  const int n = c->nbf, nocc = r->n_electrons / 2;
+  // energy-weighted density W = 2 sum_occ eps_k C_ik C_jk (same sign convention as C)
+  std::vector<double> W((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < nocc; ++k)
+        s += r->orbital_energies[k] * r->coefficient_matrix[(size_t)i * n + k] * r->coefficient_matrix[(size_t)j * n + k];
+      W[(size_t)i * n + j] = 2.0 * s;
+    }
+  return fock_gradient(c, r->density_matrix, W.data(), grad);
 }
 
 int fock_measure_fma_peak(int device, int fp64, double* gflops) {

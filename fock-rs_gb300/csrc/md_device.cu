@@ -49,26 +49,24 @@ __device__ double boys_ref_dev(double t, int n, const double* __restrict__ lut) 
 }
 
 // Accurate F_0..F_nmax by the Taylor table (see common.cuh), runtime order.
-__device__ void boys_exact_all(double T, int nmax, const double* __restrict__ tab,
-                               const double* __restrict__ etab, double* F) {
+__device__ void boys_exact_all(double T, int nmax, const double* __restrict__ tab, double* F) {
   if (T < kBoysTmax) {
-    int i = __float2int_rn((float)T * 16.0f);
+    int i = __float2int_rn((float)T * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
-    const double d = T - (double)i * 0.0625;
+    const double d = T - (double)i / kBoysPerUnit;
     const double* row = tab + ((size_t)nmax * kBoysPts + i) * kBoysTerms;
-    double f = row[kBoysTerms - 1];
-    for (int k = kBoysTerms - 2; k >= 0; --k) f = fma(f, d, row[k]);
+    double f = row[kBoysTaylor - 1];
+    for (int k = kBoysTaylor - 2; k >= 0; --k) f = fma(f, d, row[k]);
     F[nmax] = f;
     if (nmax > 0) {
       const double nd = -d;
-      double ex = fma(nd, 1.0 / 5040.0, 1.0 / 720.0);
-      ex = fma(ex, nd, 1.0 / 120.0);
+      double ex = fma(nd, 1.0 / 720.0, 1.0 / 120.0);
       ex = fma(ex, nd, 1.0 / 24.0);
       ex = fma(ex, nd, 1.0 / 6.0);
       ex = fma(ex, nd, 0.5);
       ex = fma(ex, nd, 1.0);
       ex = fma(ex, nd, 1.0);
-      ex *= etab[i];
+      ex *= row[kBoysTerms - 1];
       for (int m = nmax; m > 0; --m) F[m - 1] = (2.0 * T * F[m] + ex) / (double)(2 * m - 1);
     }
   } else {
@@ -139,7 +137,7 @@ __device__ void rtab_build(int L, double p, const double d[3], double r2, int fl
   if (flags & MD_BOYS_LUT) {
     for (int n = 0; n <= L; ++n) F[n] = boys_ref_dev(T, n, tb.ref_lut);
   } else {
-    boys_exact_all(T, L, tb.boys64, tb.exp64, F);
+    boys_exact_all(T, L, tb.boys64, F);
   }
   RTable<LMAX> nxt;
   for (int n = L; n >= 0; --n) {
@@ -173,7 +171,7 @@ __device__ double prim_overlap(const int A[3], double a, const int B[3], double 
     if (A[k] < 0 || B[k] < 0) return 0.0;
   double s = 1.0;
   for (int k = 0; k < 3; ++k) {
-    ETable<2, 4> E;
+    ETable<3, 5> E;
     etab_build(A[k], B[k], diff[k], a, b, E);
     s *= E.e[A[k]][B[k]][0];
   }
@@ -195,7 +193,104 @@ __device__ double prim_kinetic(const int A[3], double a, const int B[3], double 
   return term0 + term1 + term2;
 }
 
+// -Z 2pi/p sum E E E R(p, C - P) for any (shifted) angular vectors
+// (_nuclear_attraction, contracted_gaussian.rs:94-137); 0 for a negative one.
+__device__ double prim_nuclear(const int A[3], double a, const int B[3], double b, const double diff[3],
+                               const double P[3], const double* Cz, int flags, const MdTables& tb) {
+  for (int k = 0; k < 3; ++k)
+    if (A[k] < 0 || B[k] < 0) return 0.0;
+  const double p = a + b;
+  ETable<3, 3> E[3];
+  for (int x = 0; x < 3; ++x) etab_build(A[x], B[x], diff[x], a, b, E[x]);
+  const int L = A[0] + A[1] + A[2] + B[0] + B[1] + B[2];
+  const double dcp[3] = {Cz[0] - P[0], Cz[1] - P[1], Cz[2] - P[2]};
+  const double r2 = dcp[0] * dcp[0] + dcp[1] * dcp[1] + dcp[2] * dcp[2];
+  RTable<6> R;
+  rtab_build(L, p, dcp, r2, flags, tb, R);
+  double sum = 0.0;
+  for (int t = 0; t <= A[0] + B[0]; ++t)
+    for (int u = 0; u <= A[1] + B[1]; ++u)
+      for (int v = 0; v <= A[2] + B[2]; ++v)
+        sum += E[0].e[A[0]][B[0]][t] * E[1].e[A[1]][B[1]][u] * E[2].e[A[2]][B[2]][v] * R.at(t, u, v);
+  return -Cz[3] * (2.0 * M_PI) / p * sum;
+}
+
 }  // namespace
+
+// One-electron part of the RHF nuclear gradient for function pairs i <= j:
+//   sum_ij D_ij dH_ij/dX - W_ij dS_ij/dX
+// with d/dA phi'_a = a_x phi'_{a-1} - 2 alpha phi'_{a+1} for the reference's
+// phi' = (A - r)^a e^{-alpha |r - A|^2} functions, converted to the textbook
+// convention by the pair's sign.  The nucleus-centre derivative of V^C is
+// -(d_A + d_B) V^C (translational invariance).  D, W row-major, textbook sign.
+__global__ void one_electron_grad_kernel(const MdBasis B, const MdTables tb, const double* __restrict__ atoms,
+                                         int natom, const int* __restrict__ func_atom, int flags,
+                                         const double* __restrict__ D, const double* __restrict__ W, double* grad) {
+  const int n = B.nfunc;
+  const long long npair = (long long)n * (n + 1) / 2;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= npair) return;
+  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+  while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+  while ((long long)i * (i + 1) / 2 > t) --i;
+  const int j = (int)(t - (long long)i * (i + 1) / 2);
+  const MdFunc fa = B.funcs[j], fb = B.funcs[i];  // j <= i
+  const double diff[3] = {fb.c[0] - fa.c[0], fb.c[1] - fa.c[1], fb.c[2] - fa.c[2]};
+  const double sg = fsign(fa) * fsign(fb) * (i == j ? 1.0 : 2.0);
+  const double dij = D[(size_t)i * n + j], wij = W[(size_t)i * n + j];
+  double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+  for (int c = 0; c < natom; ++c) {
+    double gC[3] = {0, 0, 0};
+    for (int pa = 0; pa < fa.np; ++pa)
+      for (int pb = 0; pb < fb.np; ++pb) {
+        const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
+        const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb] * sg;
+        double P[3];
+        for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / (a + b);
+        for (int x = 0; x < 3; ++x) {
+          int Ap[3] = {fa.ang[0], fa.ang[1], fa.ang[2]}, Am[3] = {fa.ang[0], fa.ang[1], fa.ang[2]};
+          int Bp[3] = {fb.ang[0], fb.ang[1], fb.ang[2]}, Bm[3] = {fb.ang[0], fb.ang[1], fb.ang[2]};
+          Ap[x] += 1; Am[x] -= 1; Bp[x] += 1; Bm[x] -= 1;
+          const double vA = -2.0 * a * prim_nuclear(Ap, a, fb.ang, b, diff, P, atoms + 4 * c, flags, tb) +
+                            (double)fa.ang[x] * prim_nuclear(Am, a, fb.ang, b, diff, P, atoms + 4 * c, flags, tb);
+          const double vB = -2.0 * b * prim_nuclear(fa.ang, a, Bp, b, diff, P, atoms + 4 * c, flags, tb) +
+                            (double)fb.ang[x] * prim_nuclear(fa.ang, a, Bm, b, diff, P, atoms + 4 * c, flags, tb);
+          gA[x] += cc * dij * vA;
+          gB[x] += cc * dij * vB;
+          gC[x] -= cc * dij * (vA + vB);
+          if (c == 0) {  // overlap and kinetic once per pair
+            const double sA = -2.0 * a * prim_overlap(Ap, a, fb.ang, b, diff) +
+                              (double)fa.ang[x] * prim_overlap(Am, a, fb.ang, b, diff);
+            const double sB = -2.0 * b * prim_overlap(fa.ang, a, Bp, b, diff) +
+                              (double)fb.ang[x] * prim_overlap(fa.ang, a, Bm, b, diff);
+            const double tA = -2.0 * a * prim_kinetic(Ap, a, fb.ang, b, diff) +
+                              (double)fa.ang[x] * (fa.ang[x] > 0 ? prim_kinetic(Am, a, fb.ang, b, diff) : 0.0);
+            const double tB = -2.0 * b * prim_kinetic(fa.ang, a, Bp, b, diff) +
+                              (double)fb.ang[x] * (fb.ang[x] > 0 ? prim_kinetic(fa.ang, a, Bm, b, diff) : 0.0);
+            gA[x] += cc * (dij * tA - wij * sA);
+            gB[x] += cc * (dij * tB - wij * sB);
+          }
+        }
+      }
+    for (int x = 0; x < 3; ++x)
+      if (gC[x] != 0.0) atomicAdd(grad + 3 * c + x, gC[x]);
+  }
+  const int atA = func_atom[j], atB = func_atom[i];
+  for (int x = 0; x < 3; ++x) {
+    atomicAdd(grad + 3 * atA + x, gA[x]);
+    atomicAdd(grad + 3 * atB + x, gB[x]);
+  }
+}
+
+cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const double* atoms, int natom,
+                                 const int* func_atom, int flags, const double* D, const double* W, double* grad,
+                                 cudaStream_t s) {
+  const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
+  const int thr = 64;
+  one_electron_grad_kernel<<<(unsigned)((np + thr - 1) / thr), thr, 0, s>>>(B, tb, atoms, natom, func_atom, flags, D,
+                                                                           W, grad);
+  return cudaGetLastError();
+}
 
 // S, T, V for function pairs i <= j; one thread per pair.
 __global__ void one_electron_kernel(const MdBasis B, const MdTables tb, const double* __restrict__ atoms /*x,y,z,Z*/,

@@ -25,7 +25,6 @@ struct MdBasis {
 
 struct MdTables {
   const double* boys64;   // Taylor table (common.cuh)
-  const double* exp64;
   const double* ref_lut;  // 200 values F_10(0.15 k)
 };
 
@@ -33,6 +32,9 @@ cudaError_t md_one_electron(const MdBasis& B, const MdTables& tb, const double* 
                             double* S, double* T, double* V, cudaStream_t s);
 cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, double screen, double* diag, double* out,
                           cudaStream_t s);
+cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const double* atoms, int natom,
+                                 const int* func_atom, int flags, const double* D, const double* W, double* grad,
+                                 cudaStream_t s);
 cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* G, cudaStream_t s);
 
 }  // namespace fockgb

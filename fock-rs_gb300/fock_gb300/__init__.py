@@ -122,7 +122,23 @@ class FockContext:
         r = _lib.ScfResult()
         r.orbital_energies, r.density_matrix, r.coefficient_matrix = _dp(eps), _dp(D), _dp(Cm)
         rc = lib().fock_scf(self.handle, charge, C.byref(r))
+        self._last = (r, eps, D, Cm)  # keeps the buffers alive for energy_backward
         return rc, r, eps, D, Cm
+
+    def gradient(self, D, W) -> np.ndarray:
+        """dE/dR (natom x 3, hartree/bohr) for density D and energy-weighted density W."""
+        D = np.ascontiguousarray(D, dtype=np.float64)
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        g = np.zeros(3 * len(self.atoms))
+        check(lib().fock_gradient(self.handle, _dp(D), _dp(W), _dp(g)), "fock_gradient")
+        return g.reshape(-1, 3)
+
+    def energy_backward(self) -> np.ndarray:
+        """Gradient of the energy of the last scf() call (the energy's backward)."""
+        r = self._last[0]
+        g = np.zeros(3 * len(self.atoms))
+        check(lib().fock_energy_backward(self.handle, C.byref(r), _dp(g)), "fock_energy_backward")
+        return g.reshape(-1, 3)
 
 
 class ElectronTensor:

@@ -38,7 +38,8 @@ class Options(C.Structure):
                 ("schwarz_eps", C.c_double), ("mixed_threshold", C.c_double), ("prim_eps", C.c_double),
                 ("group_by_contraction", C.c_int), ("max_iters", C.c_int), ("epsilon", C.c_double),
                 ("conv_mode", C.c_int), ("guess", C.c_int), ("diis_len", C.c_int), ("diis_start", C.c_int),
-                ("energy_mode", C.c_int), ("final_fp64", C.c_int), ("device", C.c_int)]
+                ("energy_mode", C.c_int), ("final_fp64", C.c_int), ("device", C.c_int),
+                ("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int)]
 
 
 class ScfResult(C.Structure):
@@ -84,6 +85,8 @@ def lib():
         L.fock_one_electron.argtypes = [vp, dp, dp, dp]
         L.fock_scf.argtypes = [vp, C.c_int, C.POINTER(ScfResult)]
         L.fock_set_stream.argtypes = [vp, vp]
+        L.fock_gradient.argtypes = [vp, dp, dp, dp]
+        L.fock_energy_backward.argtypes = [vp, C.POINTER(ScfResult), dp]
         L.fock_launch_count.argtypes = [vp]
         L.fock_launch_count.restype = C.c_longlong
         L.fock_get_stats.argtypes = [vp, C.POINTER(Stats)]

@@ -89,6 +89,8 @@ typedef struct {
                       1: consistent 1/2 tr(D (2H + G(D))) */
   int final_fp64;  /* FOCK_PREC_MIXED: one FP64 Fock build + energy on the converged density */
   int device;      /* CUDA device ordinal */
+  int prims_per_slice;      /* FP64: bra primitive pairs per warp (more warps per heavy quartet) */
+  int prims_per_slice_fp32; /* same for FP32 quartets */
 } fock_options;
 
 typedef struct {
@@ -166,6 +168,19 @@ int fock_one_electron(fock_ctx* ctx, double* S, double* T, double* V);
  * FOCK_ERR_DIVERGED when the DIIS error stops being a normal number
  * (the reference's None). */
 int fock_scf(fock_ctx* ctx, int charge, fock_scf_result* result);
+
+/* RHF nuclear gradient dE/dR (no counterpart in the reference: new adjoint).
+ *   dE/dX = sum D dH/dX - sum W dS/dX + sum_unique 4 s Gam (ij|kl)^X + dVnn/dX
+ * with Gam_ijkl = D_ij D_kl - (D_ik D_jl + D_il D_jk)/4 and the energy-weighted
+ * density W = 2 sum_occ eps_k C_ik C_jk.  The derivative ERIs are formed and
+ * contracted on the fly (fused kernel, no N^4 storage).  D, W: host row-major
+ * n_basis^2 in the selected sign convention; grad: 3*natom, hartree/bohr,
+ * atom-major (x, y, z).  Exact ERI mode, shells with l <= 1. */
+int fock_gradient(fock_ctx* ctx, const double* D, const double* W, double* grad);
+
+/* Backward of fock_scf's energy: the gradient at a converged result whose
+ * density_matrix, coefficient_matrix and orbital_energies were filled. */
+int fock_energy_backward(fock_ctx* ctx, const fock_scf_result* result, double* grad);
 
 /* Use an external CUDA stream (cudaStream_t) for all work of this context;
  * NULL restores the context's own stream. */

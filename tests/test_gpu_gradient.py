@@ -1,0 +1,81 @@
+"""RHF nuclear gradient (fused derivative-ERI kernel + one-electron terms)
+against central finite differences, h = 1e-4 bohr, tolerance 1e-5 Eh/bohr."""
+import numpy as np
+import pytest
+
+from fock_gb300 import FockContext, FockError
+from fock_gb300 import _lib as L
+from fock_gb300 import basis as B
+from fock_gb300 import molecules as M
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-4
+TOL = 1e-5
+SCF = dict(guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, epsilon=1e-12, max_iters=200,
+           schwarz_eps=1e-14)
+
+
+def energy_and_gradient(basis, Zs, xyz, grad=True):
+    atoms = B.build_atoms(basis, Zs, xyz)
+    with FockContext(atoms, **SCF) as ctx:
+        rc, r, eps, D, Cm = ctx.scf(0)
+        assert rc == 0 and r.converged
+        g = ctx.energy_backward() if grad else None
+        return r.total_energy, g
+
+
+def fd_component(basis, Zs, xyz, atom, axis):
+    e = []
+    for s in (+1, -1):
+        x = np.array(xyz, dtype=float)
+        x[atom, axis] += s * H
+        e.append(energy_and_gradient(basis, Zs, x, grad=False)[0])
+    return (e[0] - e[1]) / (2 * H)
+
+
+def test_gradient_water_all_components(gpu_lib):
+    Zs, xyz = M.water_sto3g()
+    xyz = xyz + np.array([[0.0, 0.1, 0.05], [0.02, 0.0, 0.0], [0.0, 0.0, -0.03]])  # off the symmetric geometry
+    _, g = energy_and_gradient("STO-3G", Zs, xyz)
+    for atom in range(3):
+        for axis in range(3):
+            fd = fd_component("STO-3G", Zs, xyz, atom, axis)
+            assert abs(g[atom, axis] - fd) < TOL, (atom, axis, g[atom, axis], fd)
+    assert np.abs(g.sum(axis=0)).max() < 1e-9  # translational invariance
+
+
+def test_gradient_water_vs_oracle_energy_fd(gpu_lib, oracle_lib):
+    Zs, xyz = M.water_sto3g()
+    xyz = xyz + np.array([[0.0, 0.1, 0.05], [0.02, 0.0, 0.0], [0.0, 0.0, -0.03]])
+    _, g = energy_and_gradient("STO-3G", Zs, xyz)
+    for atom, axis in ((0, 2), (1, 1), (2, 0)):
+        e = []
+        for s in (+1, -1):
+            x = np.array(xyz, dtype=float)
+            x[atom, axis] += s * H
+            ob = oracle_lib.OracleBasis(B.build_atoms("STO-3G", Zs, x))
+            r, _, _ = oracle_lib.scf(ob, max_iters=200, epsilon=1e-12, eri_flags=oracle_lib.EXACT, guess=1, conv=1,
+                                     energy_mode=1, schwarz=-1.0)
+            e.append(r.total_energy)
+        fd = (e[0] - e[1]) / (2 * H)
+        assert abs(g[atom, axis] - fd) < TOL, (atom, axis, g[atom, axis], fd)
+
+
+def test_gradient_octane_fd_subset(gpu_lib):
+    Zs, xyz = M.octane(seed=0)
+    e0, g = energy_and_gradient("6-31G", Zs, xyz)
+    assert g.shape == (26, 3)
+    assert np.abs(g.sum(axis=0)).max() < 1e-8
+    for atom, axis in ((0, 0), (3, 1), (11, 2)):
+        fd = fd_component("6-31G", Zs, xyz, atom, axis)
+        assert abs(g[atom, axis] - fd) < TOL, (atom, axis, g[atom, axis], fd)
+
+
+def test_gradient_d_shells_rejected(gpu_lib):
+    Zs, xyz = M.water_cluster(1, seed=0)
+    atoms = B.build_atoms("6-31G*", Zs, xyz)
+    with FockContext(atoms, **SCF) as ctx:
+        ctx.scf(0)
+        with pytest.raises(FockError):
+            ctx.energy_backward()
