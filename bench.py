@@ -188,7 +188,7 @@ def main():
     rmx = None
     if not args.no_scf:
         t0 = time.perf_counter()
-        rmx = F.try_scf(atoms, 100, 1e-9, 0, precision=L.FOCK_PREC_MIXED, mixed_threshold=1e-4, **opts)
+        rmx = F.try_scf(atoms, 100, 1e-9, 0, precision=L.FOCK_PREC_MIXED, **opts)
         scfmx_s = time.perf_counter() - t0
         extra["scf"] = {"fp64_wall_s": scf64_s, "fp64_iterations": r64.iterations, "fp64_energy": r64.total_energy,
                         "fp64_fock_builds": r64.fock_builds, "fp64_fock_s": r64.fock_seconds,
@@ -282,19 +282,23 @@ def main():
                 "fp32_peak_tflops": fp32_peak_gflops.value / 1e3,
                 "per_class_ms": {k: round(v["ms"], 4) for k, v in sorted(per_class.items())}}
 
-    # ---- mixed precision build ----
-    ctx.set_precision(L.FOCK_PREC_MIXED, 1e-4)
+    # ---- mixed precision build (library default threshold) ----
+    th = F.options().mixed_threshold
+    ctx.set_precision(L.FOCK_PREC_MIXED, th)
     tmx = timed_builds(args.steps, args.warmup)
     ms_mx = sum(tmx) / len(tmx)
     stm = ctx.stats()
     Gm = G.clone()
-    ctx.set_precision(L.FOCK_PREC_FP64, 1e-4)
+    ctx.set_precision(L.FOCK_PREC_FP64, th)
     ctx.build_jk_device(D.data_ptr(), G.data_ptr())
     stream.synchronize()
+    # energy of one mixed build at the converged density vs the FP64 build: 1/2 sum D (G_mixed - G_fp64)
+    de_build = 0.5 * float((D * (Gm - G)).sum().item())
     mixed = {"value": nq / (ms_mx * 1e-3), "ms_per_step": ms_mx, "speedup_vs_fp64": ms / ms_mx,
-             "mixed_threshold": 1e-4, "fp32_shell_quartets": stm["shell_quartets_fp32"],
+             "mixed_threshold": th, "fp32_shell_quartets": stm["shell_quartets_fp32"],
              "fp64_shell_quartets": stm["shell_quartets_fp64"],
-             "max_abs_fock_error_vs_fp64": float((Gm - G).abs().max().item())}
+             "max_abs_fock_error_vs_fp64": float((Gm - G).abs().max().item()),
+             "single_build_energy_error_eh": abs(de_build)}
     if rmx is not None:
         mixed["abs_energy_error_vs_fp64_eh"] = abs(rmx.total_energy - r64.total_energy)
 

@@ -36,6 +36,8 @@ namespace {
 
 constexpr int kMaxL = 2;
 constexpr int kForkStreams = 8;
+// mixed-precision SCF: switch to FP64 Fock builds once max|FDS - SDF| < this
+constexpr double kMixedSwitch = 1e-4;
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
 
 inline int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
@@ -496,7 +498,7 @@ void fock_options_default(fock_options* o) {
   o->precision = FOCK_PREC_FP64;
   o->eri_mode = FOCK_ERI_EXACT;
   o->schwarz_eps = 1e-12;
-  o->mixed_threshold = 1e-4;
+  o->mixed_threshold = 1.0;
   o->prim_eps = 1e-20;
   o->group_by_contraction = 1;
   o->max_iters = 100;
@@ -1214,6 +1216,8 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   cudaEventCreate(&ev1);
   int result = FOCK_ERR_DIVERGED;
   const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
+  const double mixed_th = c->opt.mixed_threshold;
+  bool fp64_phase = false;
   for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
     cudaEventRecord(ev0, s);
     if (refc) { cku(md_g_from_tensor(c->d_tensor, Dm, n, G, s)); c->launches++; }
@@ -1260,23 +1264,20 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     bool done;
     if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) done = err < c->opt.epsilon;
     else done = iter > 0 && std::fabs(e_cur - e_prev) < c->opt.epsilon && err < std::sqrt(c->opt.epsilon);
+    if (mixed && c->opt.final_fp64 && !refc && !fp64_phase && (done || err < kMixedSwitch) &&
+        iter < c->opt.max_iters) {
+      // mixed phase close to convergence: the remaining iterations (and the
+      // reported energy) are FP64, so the result carries no FP32 error
+      int r = fock_set_precision(c, FOCK_PREC_FP64, c->opt.mixed_threshold);
+      if (r != FOCK_OK) { fail = r; break; }
+      fp64_phase = true;
+      e_prev = e_cur;
+      std::swap(Dm, Dn);
+      continue;
+    }
     if (done || iter == c->opt.max_iters) {
       double e_report = c->opt.energy_mode == 0 ? e_ref : e_cur;
       const double* Dfinal = c->opt.energy_mode == 0 ? Dn : Dm;
-      if (mixed && c->opt.final_fp64 && !refc) {
-        // refinement: one FP64 build on the converged density, consistent energy
-        fock_options keep = c->opt;
-        int r = fock_set_precision(c, FOCK_PREC_FP64, keep.mixed_threshold);
-        if (r == FOCK_OK) r = fock_build_jk_device(c, Dfinal, G);
-        builds++;
-        cku(cudaMemsetAsync(scal, 0, 8, s));
-        cku(k_energy(Dfinal, H, G, (int)nn, scal, s));
-        cku(cudaMemcpyAsync(hs, scal, 8, cudaMemcpyDeviceToHost, s));
-        cku(cudaStreamSynchronize(s));
-        fock_set_precision(c, FOCK_PREC_MIXED, keep.mixed_threshold);
-        if (r != FOCK_OK) { fail = r; break; }
-        e_report = hs[0];
-      }
       res->electronic_energy = e_report;
       res->total_energy = e_report + vnn;
       res->nuclear_repulsion = vnn;
@@ -1308,6 +1309,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     e_prev = e_cur;
     std::swap(Dm, Dn);
   }
+  if (fp64_phase) fock_set_precision(c, FOCK_PREC_MIXED, mixed_th);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   res->fock_seconds = fock_ms * 1e-3;

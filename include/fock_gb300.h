@@ -87,7 +87,8 @@ typedef struct {
   int diis_start; /* 5  (scf/src/lib.rs:202) */
   int energy_mode; /* 0: reference 1/2 tr(D_new (2H + G(D_old))) (scf/src/lib.rs:223);
                       1: consistent 1/2 tr(D (2H + G(D))) */
-  int final_fp64;  /* FOCK_PREC_MIXED: one FP64 Fock build + energy on the converged density */
+  int final_fp64;  /* FOCK_PREC_MIXED: finish the SCF with FP64 Fock builds once
+                      max|FDS - SDF| < 1e-4, so the energy carries no FP32 error */
   int device;      /* CUDA device ordinal */
   int prims_per_slice;      /* FP64: bra primitive pairs per warp (more warps per heavy quartet) */
   int prims_per_slice_fp32; /* same for FP32 quartets */
@@ -112,7 +113,7 @@ typedef struct {
 typedef struct fock_ctx fock_ctx;
 
 /* Defaults: reference sign convention, FP64, exact ERIs, schwarz 1e-12,
- * mixed threshold 1e-4, prim_eps 1e-20, grouping on, SCF 100 iterations,
+ * mixed threshold 1.0, prim_eps 1e-20, grouping on, SCF 100 iterations,
  * epsilon 1e-6, commutator convergence, GWH guess, DIIS 16/5, energy_mode 0. */
 void fock_options_default(fock_options* opt);
 
