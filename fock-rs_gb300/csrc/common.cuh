@@ -38,6 +38,8 @@ struct PairInfo {
   int cls;        // pair class index
   double AB[3];   // A - B
   int atom_a, atom_b;  // centres of shells a and b (gradient)
+  int mol_off;    // offset of this molecule's n x n block in D, M, G (batches)
+  int mol_n;      // basis size of this molecule: row stride of that block
 };
 
 // Primitive pair, double: {p, 1/(2p)}, {K, Px}, {Py, Pz}, {PAx, PAy},
@@ -65,21 +67,23 @@ struct __align__(16) ExpPair32 {
 };
 
 // One launch of one class: rows are bra pairs; row r covers the kets
-// ket_list[row_beg[r] .. row_beg[r] + row_cnt[r]); each warp takes one row,
-// 32 consecutive kets and one of row_slices[r] slices of the bra primitive
-// pairs (the recurrences after the primitive loop are linear, so every slice
-// digests its partial sums on its own); row_warp_off is the exclusive prefix
-// sum of ceil(row_cnt / 32) * row_slices.  Schwarz mode: bra_list holds
-// nrows pairs, one per thread.
+// ket_list[row_beg[r] .. row_beg[r] + row_cnt[r]) and row_slices[r] slices
+// of the bra primitive pairs (the recurrences after the primitive loop are
+// linear, so every slice digests its partial sums on its own).  Lanes are
+// packed densely: lane t of the launch takes row r with
+// row_off[r] <= t < row_off[r+1] (row_off: prefix sum of row_cnt * row_slices),
+// slice (t - row_off[r]) / row_cnt[r] and the ket at the remainder, so every
+// warp is full except the launch's last.  Schwarz mode: bra_list holds nrows
+// pairs, one per thread.
 struct ClassLaunch {
   const int* bra_list;
   const int* ket_list;
   const int* row_beg;
   const int* row_cnt;
   const int* row_slices;
-  const long long* row_warp_off;
+  const long long* row_off;
   int nrows;
-  long long nwarps;
+  long long nlanes;
 };
 
 struct EriArgs {

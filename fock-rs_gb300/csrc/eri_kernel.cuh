@@ -80,11 +80,15 @@ template <>
 __device__ __forceinline__ const float* boys_table<float>(const EriArgs& a) { return a.boys32; }
 
 template <typename R>
-__device__ __forceinline__ R dens(const EriArgs& a, int i, int j);
+__device__ __forceinline__ R dens(const EriArgs& a, size_t mo, int ld, int i, int j);
 template <>
-__device__ __forceinline__ double dens<double>(const EriArgs& a, int i, int j) { return __ldg(a.D + (size_t)i * a.nbf + j); }
+__device__ __forceinline__ double dens<double>(const EriArgs& a, size_t mo, int ld, int i, int j) {
+  return __ldg(a.D + mo + (size_t)i * ld + j);
+}
 template <>
-__device__ __forceinline__ float dens<float>(const EriArgs& a, int i, int j) { return __ldg(a.D32 + (size_t)i * a.nbf + j); }
+__device__ __forceinline__ float dens<float>(const EriArgs& a, size_t mo, int ld, int i, int j) {
+  return __ldg(a.D32 + mo + (size_t)i * ld + j);
+}
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -95,6 +99,23 @@ __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
+__device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, int& bra, int& ket, int& slice,
+                                            int& nslice) {
+  int lo = 0, hi = cl.nrows - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(cl.row_off + mid) <= t) lo = mid; else hi = mid - 1;
+  }
+  const long long local = t - __ldg(cl.row_off + lo);
+  const int cnt = __ldg(cl.row_cnt + lo);
+  nslice = __ldg(cl.row_slices + lo);
+  slice = (int)(local / cnt);
+  const int k = (int)(local - (long long)slice * cnt);
+  bra = __ldg(cl.bra_list + lo);
+  ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
 }
 
 template <class C, typename R, int MODE>
@@ -109,22 +130,12 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
   } else {
-    const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (gw >= cl.nwarps) return;  // uniform per warp
-    int lo = 0, hi = cl.nrows - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(cl.row_warp_off + mid) <= gw) lo = mid; else hi = mid - 1;
-    }
-    const int w = (int)(gw - __ldg(cl.row_warp_off + lo));
-    nslice = cl.row_slices ? __ldg(cl.row_slices + lo) : 1;
-    slice = w % nslice;
-    const int k = (w / nslice) * 32 + lane;
-    const int cnt = __ldg(cl.row_cnt + lo);
-    active = k < cnt;
-    bra = __ldg(cl.bra_list + lo);
-    ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + (active ? k : 0));
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
+    decode_lane(cl, t, bra, ket, slice, nslice);
+    active = true;
   }
+  (void)lane;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
   // this warp's slice of the bra primitive pairs
@@ -179,6 +190,8 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   }
 
   const int fa = Pb.fa, fb = Pb.fb, fc = Pk.fa, fd = Pk.fb;
+  const size_t mo = (size_t)Pb.mol_off;  // molecule block (all four shells share it)
+  const int ld = Pb.mol_n;
   if (MODE == MODE_SCHWARZ) {
     if (!active) return;
     double q = 0.0;
@@ -223,24 +236,24 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
 #pragma unroll
     for (int ia = 0; ia < NA; ++ia)
 #pragma unroll
-      for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = dens<R>(a, fa + ia, fb + ib);
+      for (int ib = 0; ib < NB; ++ib) Dab[ia * NB + ib] = dens<R>(a, mo, ld, fa + ia, fb + ib);
 #pragma unroll
     for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-      for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = dens<R>(a, fc + ic, fd + id);
+      for (int id = 0; id < ND; ++id) Dcd[ic * ND + id] = dens<R>(a, mo, ld, fc + ic, fd + id);
 #pragma unroll
     for (int ia = 0; ia < NA; ++ia) {
 #pragma unroll
-      for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = dens<R>(a, fa + ia, fc + ic);
+      for (int ic = 0; ic < NC; ++ic) Dac[ia * NC + ic] = dens<R>(a, mo, ld, fa + ia, fc + ic);
 #pragma unroll
-      for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = dens<R>(a, fa + ia, fd + id);
+      for (int id = 0; id < ND; ++id) Dad[ia * ND + id] = dens<R>(a, mo, ld, fa + ia, fd + id);
     }
 #pragma unroll
     for (int ib = 0; ib < NB; ++ib) {
 #pragma unroll
-      for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = dens<R>(a, fb + ib, fc + ic);
+      for (int ic = 0; ic < NC; ++ic) Dbc[ib * NC + ic] = dens<R>(a, mo, ld, fb + ib, fc + ic);
 #pragma unroll
-      for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = dens<R>(a, fb + ib, fd + id);
+      for (int id = 0; id < ND; ++id) Dbd[ib * ND + id] = dens<R>(a, mo, ld, fb + ib, fd + id);
     }
 #pragma unroll
     for (int i = 0; i < NC * ND; ++i) jcd[i] = R(0);
@@ -271,32 +284,26 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   }
   const double sdeg = (Pb.sa == Pb.sb ? 0.5 : 1.0) * (Pk.sa == Pk.sb ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
   const double sj = 2.0 * sdeg, sk = -0.5 * sdeg;
-  const size_t n = (size_t)a.nbf;
-  // bra J block: identical bra across the warp -> shuffle-reduce, one atomic per element
-#pragma unroll
-  for (int i = 0; i < NA * NB; ++i) {
-    double v = (double)jab[i] * (active ? sj : 0.0);
-    v = warp_sum(v);
-    if (lane == 0 && v != 0.0) atomicAdd(a.M + (size_t)(fa + i / NB) * n + (fb + i % NB), v);
-  }
   if (!active) return;
+#pragma unroll
+  for (int i = 0; i < NA * NB; ++i) atomicAdd(a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB), sj * (double)jab[i]);
 #pragma unroll
   for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fc + ic) * n + (fd + id), sj * (double)jcd[ic * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fc + ic) * ld + (fd + id), sj * (double)jcd[ic * ND + id]);
 #pragma unroll
   for (int ia = 0; ia < NA; ++ia) {
 #pragma unroll
-    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + (size_t)(fa + ia) * n + (fc + ic), sk * (double)kac[ia * NC + ic]);
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fc + ic), sk * (double)kac[ia * NC + ic]);
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fa + ia) * n + (fd + id), sk * (double)kad[ia * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fd + id), sk * (double)kad[ia * ND + id]);
   }
 #pragma unroll
   for (int ib = 0; ib < NB; ++ib) {
 #pragma unroll
-    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + (size_t)(fb + ib) * n + (fc + ic), sk * (double)kbc[ib * NC + ic]);
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fc + ic), sk * (double)kbc[ib * NC + ic]);
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + (size_t)(fb + ib) * n + (fd + id), sk * (double)kbd[ib * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fd + id), sk * (double)kbd[ib * ND + id]);
   }
 }
 
@@ -311,21 +318,11 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
 template <class C>
 __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch cl, const EriArgs a) {
   constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, LG = C::LG;
-  const int lane = threadIdx.x & 31;
-  const long long gw = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (gw >= cl.nwarps) return;
-  int lo = 0, hi = cl.nrows - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (__ldg(cl.row_warp_off + mid) <= gw) lo = mid; else hi = mid - 1;
-  }
-  const int w = (int)(gw - __ldg(cl.row_warp_off + lo));
-  const int nslice = cl.row_slices ? __ldg(cl.row_slices + lo) : 1;
-  const int slice = w % nslice;
-  const int k = (w / nslice) * 32 + lane;
-  const bool active = k < __ldg(cl.row_cnt + lo);
-  const int bra = __ldg(cl.bra_list + lo);
-  const int ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + (active ? k : 0));
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= cl.nlanes) return;
+  int bra, ket, slice, nslice;
+  decode_lane(cl, t, bra, ket, slice, nslice);
+  const bool active = true;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
   const int ib0 = (int)(((long long)slice * Pb.nprim) / nslice);
@@ -368,6 +365,8 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
   double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0}, gC[3] = {0, 0, 0};
   if (active) {
     const int fa = Pb.fa, fb = Pb.fb, fc = Pk.fa, fd = Pk.fb;
+    const size_t mo = (size_t)Pb.mol_off;
+    const int ld = Pb.mol_n;
     double gam[NA * NB * NC * ND];
 #pragma unroll
     for (int ia = 0; ia < NA; ++ia)
@@ -377,9 +376,9 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
         for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
           for (int id = 0; id < ND; ++id) {
-            const double dab = dens<double>(a, fa + ia, fb + ib), dcd = dens<double>(a, fc + ic, fd + id);
-            const double dac = dens<double>(a, fa + ia, fc + ic), dbd = dens<double>(a, fb + ib, fd + id);
-            const double dad = dens<double>(a, fa + ia, fd + id), dbc = dens<double>(a, fb + ib, fc + ic);
+            const double dab = dens<double>(a, mo, ld, fa + ia, fb + ib), dcd = dens<double>(a, mo, ld, fc + ic, fd + id);
+            const double dac = dens<double>(a, mo, ld, fa + ia, fc + ic), dbd = dens<double>(a, mo, ld, fb + ib, fd + id);
+            const double dad = dens<double>(a, mo, ld, fa + ia, fd + id), dbc = dens<double>(a, mo, ld, fb + ib, fc + ic);
             gam[((ia * NB + ib) * NC + ic) * ND + id] =
                 (dab * dcd - 0.25 * (dac * dbd + dad * dbc)) *
                 (comp_factor(C::LA, ia) * comp_factor(C::LB, ib) * comp_factor(C::LC, ic) * comp_factor(C::LD, id));
@@ -393,18 +392,10 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
 #pragma unroll
     for (int i = 0; i < 3; ++i) { gA[i] = sdeg * g[i]; gB[i] = sdeg * g[3 + i]; gC[i] = sdeg * g[6 + i]; }
   }
-  // bra centres are uniform across the warp: reduce first
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const double sa = warp_sum(gA[i]), sb = warp_sum(gB[i]);
-    if (lane == 0) {
-      if (sa != 0.0) atomicAdd(a.grad + 3 * Pb.atom_a + i, sa);
-      if (sb != 0.0) atomicAdd(a.grad + 3 * Pb.atom_b + i, sb);
-    }
-  }
-  if (!active) return;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
+    atomicAdd(a.grad + 3 * Pb.atom_a + i, gA[i]);
+    atomicAdd(a.grad + 3 * Pb.atom_b + i, gB[i]);
     atomicAdd(a.grad + 3 * Pk.atom_a + i, gC[i]);
     atomicAdd(a.grad + 3 * Pk.atom_b + i, -(gA[i] + gB[i] + gC[i]));
   }
@@ -414,8 +405,8 @@ template <class C>
 cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
   if (mode == MODE_GRAD) {
     if constexpr (C::HAS_GRAD) {
-      if (cl.nwarps <= 0) return cudaSuccess;
-      const long long blocks = (cl.nwarps * 32 + kEriThreads - 1) / kEriThreads;
+      if (cl.nlanes <= 0) return cudaSuccess;
+      const long long blocks = (cl.nlanes + kEriThreads - 1) / kEriThreads;
       if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
       eri_grad_kernel<C><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
       return cudaGetLastError();
@@ -433,9 +424,8 @@ cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int 
       return cudaErrorInvalidValue;
     }
   }
-  if (cl.nwarps <= 0) return cudaSuccess;
-  const long long threads = cl.nwarps * 32;
-  const long long blocks = (threads + kEriThreads - 1) / kEriThreads;
+  if (cl.nlanes <= 0) return cudaSuccess;
+  const long long blocks = (cl.nlanes + kEriThreads - 1) / kEriThreads;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   if (mode == MODE_TENSOR) {
     eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);

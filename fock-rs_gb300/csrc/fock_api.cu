@@ -108,7 +108,8 @@ double prim_norm(int i, int j, int k, double alpha) {
 }
 
 struct HostShell {
-  int l, atom, nprim, f0;
+  int l, atom, nprim, f0;  // f0: first function of the shell within its molecule
+  int mol = 0;
   double c[3];
   std::vector<double> exps, coefs;  // coefs normalised for the x^l component
 };
@@ -178,6 +179,13 @@ struct fock_ctx {
   int* d_plan_int = nullptr;
   long long* d_plan_ll = nullptr;
   fock_stats stats{};
+  // molecules (one for fock_ctx_create, many for a batch)
+  int nmol = 1;
+  std::vector<int> mol_shell0, mol_nbf, mol_f0;
+  std::vector<long long> mol_off;  // nmol + 1 block offsets
+  long long total_elems = 0;
+  long long* d_mol_off = nullptr;
+  int* d_mol_n = nullptr;
   // MD basis (one-electron, refcompat tensor)
   MdFunc* d_mdfuncs = nullptr;
   double *d_mdexps = nullptr, *d_mdcoefs = nullptr, *d_atoms4 = nullptr;
@@ -265,15 +273,17 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   const bool mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
   const double tmix = c->opt.mixed_threshold;
   const int npairs = (int)c->hpairs.size();
-  // pairs per class, sorted by Q descending (ties by index for determinism)
-  std::vector<std::vector<int>> cls(kNumPairClasses);
+  const int nmol = c->nmol;
+  // pairs per (molecule, class), sorted by Q descending (ties by index)
+  std::vector<std::vector<std::vector<int>>> cls(nmol, std::vector<std::vector<int>>(kNumPairClasses));
   for (int p = 0; p < npairs; ++p)
-    if (c->hpairs[p].nprim > 0) cls[c->hpairs[p].cls].push_back(p);
+    if (c->hpairs[p].nprim > 0) cls[c->shells[c->hpairs[p].sa].mol][c->hpairs[p].cls].push_back(p);
   std::vector<int> rank(npairs, -1);
-  for (auto& v : cls) {
-    std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return c->Q[a] > c->Q[b]; });
-    for (size_t r = 0; r < v.size(); ++r) rank[v[r]] = (int)r;
-  }
+  for (auto& mc : cls)
+    for (auto& v : mc) {
+      std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return c->Q[a] > c->Q[b]; });
+      for (size_t r = 0; r < v.size(); ++r) rank[v[r]] = (int)r;
+    }
   std::vector<int> ints;
   std::vector<long long> lls;
   struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
@@ -281,88 +291,91 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   fock_stats st{};
   st.shell_pairs = npairs;
   st.prim_pairs = c->nprim_pairs;
-  const long long nfp = (long long)c->nbf * (c->nbf + 1) / 2;
-  st.function_quartets_unique = nfp * (nfp + 1) / 2;
-  // every shell quartet of the basis (pairs whose primitive pairs were all
-  // dropped count as screened)
+  // every shell quartet of every molecule (pairs whose primitive pairs were
+  // all dropped count as screened)
   long long total_shell_quartets = 0;
-  {
+  for (int m = 0; m < nmol; ++m) {
+    const long long nf = c->mol_nbf[m], nfp = nf * (nf + 1) / 2;
+    st.function_quartets_unique += nfp * (nfp + 1) / 2;
     std::vector<long long> ncls(kNumPairClasses, 0);
-    for (const PairInfo& p : c->hpairs) ncls[p.cls]++;
+    for (const PairInfo& p : c->hpairs)
+      if (c->shells[p.sa].mol == m) ncls[p.cls]++;
     for (int X = 0; X < kNumPairClasses; ++X)
       for (int Y = 0; Y <= X; ++Y) total_shell_quartets += (X == Y) ? ncls[X] * (ncls[X] + 1) / 2 : ncls[X] * ncls[Y];
   }
   for (int X = 0; X < kNumPairClasses; ++X) {
-    if (cls[X].empty()) continue;
     for (int Y = 0; Y <= X; ++Y) {
-      if (cls[Y].empty()) continue;
       int la = 0, lb = 0, lc = 0, ld = 0;
       for (int a = 0; a <= kMaxL; ++a)
         for (int b = 0; b <= a; ++b) {
           if (pair_class(a, b) == X) { la = a; lb = b; }
           if (pair_class(a, b) == Y) { lc = a; ld = b; }
         }
-      const std::vector<int>& bras = cls[X];
-      const std::vector<int>& kall = cls[Y];
-      // ket groups (by primitive-pair count) keep the Q order
-      std::vector<std::vector<int>> groups;
+      // ket groups by primitive-pair count (uniform inner loops); -1 = all
+      std::vector<int> keys;
       if (c->opt.group_by_contraction) {
-        std::vector<int> keys;
-        for (int p : kall) keys.push_back(c->hpairs[p].nprim);
+        for (int m = 0; m < nmol; ++m)
+          for (int p : cls[m][Y]) keys.push_back(c->hpairs[p].nprim);
         std::sort(keys.begin(), keys.end());
         keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
-        for (int k : keys) {
-          std::vector<int> g;
-          for (int p : kall) if (c->hpairs[p].nprim == k) g.push_back(p);
-          groups.push_back(g);
-        }
       } else {
-        groups.push_back(kall);
+        keys.push_back(-1);
       }
       int hrr = 0, neri = 0;
       const int vrr = class_vrr_flops(la, lb, lc, ld, &hrr, &neri);
-      const int L = la + lb + lc + ld;
-      for (auto& g : groups) {
-        std::vector<float> gq(g.size());
-        std::vector<int> grank(g.size());
-        std::vector<long long> gprim(g.size() + 1, 0);
-        for (size_t k = 0; k < g.size(); ++k) {
-          gq[k] = c->Q[g[k]];
-          grank[k] = rank[g[k]];
-          gprim[k + 1] = gprim[k] + c->hpairs[g[k]].nprim;
-        }
+      for (int key : keys) {
         for (int prec = 0; prec < (mixed ? 2 : 1); ++prec) {
-          std::vector<int> rbra, rbeg, rcnt;
+          std::vector<int> rbra, rbeg, rcnt, kets;
           long long q = 0, pq = 0;
-          for (int bi : bras) {
-            const double Qb = c->Q[bi];
-            // count of kets allowed by the canonical order (same class: rank <= rank(bra))
-            size_t n_order = g.size();
-            if (X == Y) n_order = std::upper_bound(grank.begin(), grank.end(), rank[bi]) - grank.begin();
-            // Schwarz: Q_b Q_k >= tau  (gq descending)
-            auto cnt_ge = [&](double thr) -> size_t {
-              if (thr <= 0.0) return g.size();
-              if (Qb <= 0.0) return 0;
-              const double need = thr / Qb;
-              size_t lo = 0, hi = g.size();
-              while (lo < hi) {
-                size_t mid = (lo + hi) / 2;
-                if ((double)gq[mid] >= need) lo = mid + 1; else hi = mid;
-              }
-              return lo;
-            };
-            size_t n_all = std::min(n_order, cnt_ge(tau));
-            size_t beg = 0, end = n_all;
-            if (mixed) {
-              size_t n64 = std::min(n_all, cnt_ge(tmix));
-              if (prec == 0) end = n64; else beg = n64;
+          for (int m = 0; m < nmol; ++m) {
+            const std::vector<int>& bras = cls[m][X];
+            if (bras.empty() || cls[m][Y].empty()) continue;
+            std::vector<int> g;  // this molecule's kets of the group, Q order
+            for (int p : cls[m][Y])
+              if (key < 0 || c->hpairs[p].nprim == key) g.push_back(p);
+            if (g.empty()) continue;
+            std::vector<float> gq(g.size());
+            std::vector<int> grank(g.size());
+            std::vector<long long> gprim(g.size() + 1, 0);
+            for (size_t k = 0; k < g.size(); ++k) {
+              gq[k] = c->Q[g[k]];
+              grank[k] = rank[g[k]];
+              gprim[k + 1] = gprim[k] + c->hpairs[g[k]].nprim;
             }
-            if (end <= beg) continue;
-            rbra.push_back(bi);
-            rbeg.push_back((int)beg);
-            rcnt.push_back((int)(end - beg));
-            q += (long long)(end - beg);
-            pq += (long long)c->hpairs[bi].nprim * (gprim[end] - gprim[beg]);
+            const int base = (int)kets.size();
+            bool used = false;
+            for (int bi : bras) {
+              const double Qb = c->Q[bi];
+              // kets allowed by the canonical order (same class: rank <= rank(bra))
+              size_t n_order = g.size();
+              if (X == Y) n_order = std::upper_bound(grank.begin(), grank.end(), rank[bi]) - grank.begin();
+              // Schwarz: Q_b Q_k >= threshold  (gq descending)
+              auto cnt_ge = [&](double thr) -> size_t {
+                if (thr <= 0.0) return g.size();
+                if (Qb <= 0.0) return 0;
+                const double need = thr / Qb;
+                size_t lo = 0, hi = g.size();
+                while (lo < hi) {
+                  size_t mid = (lo + hi) / 2;
+                  if ((double)gq[mid] >= need) lo = mid + 1; else hi = mid;
+                }
+                return lo;
+              };
+              size_t n_all = std::min(n_order, cnt_ge(tau));
+              size_t beg = 0, end = n_all;
+              if (mixed) {
+                size_t n64 = std::min(n_all, cnt_ge(tmix));
+                if (prec == 0) end = n64; else beg = n64;
+              }
+              if (end <= beg) continue;
+              used = true;
+              rbra.push_back(bi);
+              rbeg.push_back(base + (int)beg);
+              rcnt.push_back((int)(end - beg));
+              q += (long long)(end - beg);
+              pq += (long long)c->hpairs[bi].nprim * (gprim[end] - gprim[beg]);
+            }
+            if (used) kets.insert(kets.end(), g.begin(), g.end());
           }
           if (rbra.empty()) continue;
           Pending P{};
@@ -373,9 +386,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           P.bra = ints.size();
           ints.insert(ints.end(), rbra.begin(), rbra.end());
           P.ket = ints.size();
-          ints.insert(ints.end(), g.begin(), g.end());
+          ints.insert(ints.end(), kets.begin(), kets.end());
           P.beg = ints.size();
-          // row_beg indexes the shared ket list of this group
           ints.insert(ints.end(), rbeg.begin(), rbeg.end());
           P.cnt = ints.size();
           ints.insert(ints.end(), rcnt.begin(), rcnt.end());
@@ -388,13 +400,13 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           ints.insert(ints.end(), rsl.begin(), rsl.end());
           P.off = lls.size();
           long long acc = 0;
-          for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)((rcnt[r] + 31) / 32) * rsl[r]; }
+          for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)rcnt[r] * rsl[r]; }
           lls.push_back(acc);
           P.p.cl.nrows = (int)rbra.size();
-          P.p.cl.nwarps = acc;
-          pend.push_back(P);
+          P.p.cl.nlanes = acc;
           const long long flops = pq * ((long long)vrr + setup_flops(la, lb, lc, ld)) + q * ((long long)hrr + 12LL * neri);
-          pend.back().p.flops = flops;
+          P.p.flops = flops;
+          pend.push_back(P);
           if (P.p.prec == PREC_FP32) {
             st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
           } else {
@@ -415,7 +427,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.row_beg = c->d_plan_int + P.beg;
     P.p.cl.row_cnt = c->d_plan_int + P.cnt;
     P.p.cl.row_slices = c->d_plan_int + P.sl;
-    P.p.cl.row_warp_off = c->d_plan_ll + P.off;
+    P.p.cl.row_off = c->d_plan_ll + P.off;
     c->plans.push_back(P.p);
   }
   st.launches_per_build = (int)c->plans.size() + 1;
@@ -489,6 +501,9 @@ int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri) {
 }
 }  // namespace
 
+int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell, const fock_options* opt,
+               const int* mol_shell_begin, int nmol, fock_ctx** out);
+
 extern "C" {
 
 void fock_options_default(fock_options* o) {
@@ -556,6 +571,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
   dfree(c->d_plan_int); dfree(c->d_plan_ll);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
+  dfree(c->d_mol_off); dfree(c->d_mol_n);
   dfree(c->d_tensor);
   if (c->blas) cublasDestroy(c->blas);
   if (c->solver) cusolverDnDestroy(c->solver);
@@ -572,9 +588,24 @@ void fock_ctx_destroy(fock_ctx* c) {
 
 int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell, const fock_options* opt,
                     fock_ctx** out) {
+  const int begin[2] = {0, nshell};
+  return create_ctx(atoms, natom, shells, nshell, opt, begin, 1, out);
+}
+
+}  // extern "C"
+
+// Context over nmol molecules: molecule m owns shells
+// [mol_shell_begin[m], mol_shell_begin[m+1]) (atom indices are global);
+// shell pairs and quartets never mix molecules, and every molecule has its
+// own n_m x n_m block in D, M and G (offsets mol_off).
+int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell, const fock_options* opt,
+               const int* mol_shell_begin, int nmol, fock_ctx** out) {
   if (!out) return FOCK_ERR_INVALID_ARG;
   *out = nullptr;
-  if (!atoms || natom <= 0 || !shells || nshell <= 0) return FOCK_ERR_INVALID_ARG;
+  if (!atoms || natom <= 0 || !shells || nshell <= 0 || nmol <= 0 || !mol_shell_begin) return FOCK_ERR_INVALID_ARG;
+  if (mol_shell_begin[0] != 0 || mol_shell_begin[nmol] != nshell) return FOCK_ERR_INVALID_ARG;
+  for (int m = 0; m < nmol; ++m)
+    if (mol_shell_begin[m + 1] <= mol_shell_begin[m]) return FOCK_ERR_INVALID_ARG;
   fock_options o;
   if (opt) o = *opt; else fock_options_default(&o);
   for (int s = 0; s < nshell; ++s) {
@@ -598,21 +629,36 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
   c->device = o.device;
   c->natom = natom;
   c->atoms.assign(atoms, atoms + natom);
-  int f0 = 0;
-  for (int s = 0; s < nshell; ++s) {
-    const fock_shell& sh = shells[s];
-    HostShell h;
-    h.l = sh.l; h.atom = sh.atom; h.nprim = sh.nprim; h.f0 = f0;
-    h.c[0] = atoms[sh.atom].x; h.c[1] = atoms[sh.atom].y; h.c[2] = atoms[sh.atom].z;
-    for (int k = 0; k < sh.nprim; ++k) {
-      h.exps.push_back(sh.exps[k]);
-      h.coefs.push_back(sh.coefs[k] * prim_norm(sh.l, 0, 0, sh.exps[k]));
+  c->nmol = nmol;
+  c->mol_shell0.assign(mol_shell_begin, mol_shell_begin + nmol + 1);
+  int gf = 0;
+  long long off = 0;
+  for (int m = 0; m < nmol; ++m) {
+    int f0 = 0;
+    for (int s = mol_shell_begin[m]; s < mol_shell_begin[m + 1]; ++s) {
+      const fock_shell& sh = shells[s];
+      HostShell h;
+      h.l = sh.l; h.atom = sh.atom; h.nprim = sh.nprim; h.f0 = f0; h.mol = m;
+      h.c[0] = atoms[sh.atom].x; h.c[1] = atoms[sh.atom].y; h.c[2] = atoms[sh.atom].z;
+      for (int k = 0; k < sh.nprim; ++k) {
+        h.exps.push_back(sh.exps[k]);
+        h.coefs.push_back(sh.coefs[k] * prim_norm(sh.l, 0, 0, sh.exps[k]));
+      }
+      f0 += ncart(sh.l);
+      for (int k = 0; k < ncart(sh.l); ++k) c->fsign.push_back((sh.l & 1) ? -1.0 : 1.0);
+      c->shells.push_back(h);
     }
-    f0 += ncart(sh.l);
-    for (int k = 0; k < ncart(sh.l); ++k) c->fsign.push_back((sh.l & 1) ? -1.0 : 1.0);
-    c->shells.push_back(h);
+    c->mol_nbf.push_back(f0);
+    c->mol_f0.push_back(gf);
+    c->mol_off.push_back(off);
+    gf += f0;
+    off += (long long)f0 * f0;
   }
-  c->nbf = f0;
+  c->mol_off.push_back(off);
+  c->mol_f0.push_back(gf);
+  c->total_elems = off;
+  if (off > 0x7fffffffLL) { delete c; return FOCK_ERR_TOO_LARGE; }
+  c->nbf = gf;  // total functions (the basis size for one molecule)
   int rc = FOCK_OK;
   auto fail = [&](int code) { fock_ctx_destroy(c); return code; };
   if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return fail(FOCK_ERR_CUDA);
@@ -630,7 +676,7 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
   std::vector<PrimPair32> p32;
   const double kpref = std::sqrt(2.0) * std::pow(M_PI, 1.25);
   for (int i = 0; i < nshell; ++i)
-    for (int j = 0; j <= i; ++j) {
+    for (int j = c->mol_shell0[c->shells[i].mol]; j <= i; ++j) {
       int a = i, b = j;
       if (c->shells[j].l > c->shells[i].l) { a = j; b = i; }
       const HostShell &A = c->shells[a], &B = c->shells[b];
@@ -638,6 +684,8 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       P.prim_off = (int)p64.size();
       P.fa = A.f0; P.fb = B.f0; P.sa = a; P.sb = b;
       P.atom_a = A.atom; P.atom_b = B.atom;
+      P.mol_off = (int)c->mol_off[A.mol];
+      P.mol_n = c->mol_nbf[A.mol];
       P.cls = pair_class(A.l, B.l);
       for (int k = 0; k < 3; ++k) P.AB[k] = A.c[k] - B.c[k];
       const double ab2 = P.AB[0] * P.AB[0] + P.AB[1] * P.AB[1] + P.AB[2] * P.AB[2];
@@ -700,7 +748,7 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       xp32[(size_t)i * c->nxp + j] = ExpPair32{(float)e.rs, (float)e.inv, (float)e.rp, (float)e.rq};
     }
   const int npairs = (int)c->hpairs.size();
-  const size_t nn = (size_t)c->nbf * c->nbf;
+  const size_t nn = (size_t)c->total_elems;  // all molecule blocks
   if ((rc = map_cuda(dalloc(&c->d_pairs, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_prim64, p64.size()))) ||
       (rc = map_cuda(dalloc(&c->d_prim32, p32.size()))) ||
@@ -763,11 +811,21 @@ int fock_ctx_create(const fock_atom* atoms, int natom, const fock_shell* shells,
       return fail(rc);
   }
 
+  {
+    std::vector<int> mn(c->mol_nbf.begin(), c->mol_nbf.end());
+    if ((rc = map_cuda(dalloc(&c->d_mol_off, c->mol_off.size()))) || (rc = map_cuda(dalloc(&c->d_mol_n, mn.size()))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_mol_off, c->mol_off.data(), c->mol_off.size() * sizeof(long long),
+                                  cudaMemcpyHostToDevice))) ||
+        (rc = map_cuda(cudaMemcpy(c->d_mol_n, mn.data(), mn.size() * sizeof(int), cudaMemcpyHostToDevice))))
+      return fail(rc);
+  }
   if ((rc = compute_schwarz(c)) != FOCK_OK) return fail(rc);
   if ((rc = build_plan(c, false)) != FOCK_OK) return fail(rc);
   *out = c;
   return FOCK_OK;
 }
+
+extern "C" {
 
 int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
   if (!c || (precision != FOCK_PREC_FP64 && precision != FOCK_PREC_MIXED) || !(mixed_threshold >= 0.0))
@@ -785,8 +843,7 @@ int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
 // G = M + M^T.  Captured once per plan, replayed per build.
 static int capture_jk_graph(fock_ctx* c) {
   if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
-  const int n = c->nbf;
-  const size_t nn = (size_t)n * n;
+  const size_t nn = (size_t)c->total_elems;
   cudaStream_t cs = c->cap_stream;
   EriArgs a = eri_args(c);
   bool need32 = false;
@@ -810,7 +867,10 @@ static int capture_jk_graph(fock_ctx* c) {
     e = cudaEventRecord(c->join_ev[s], c->side[s]);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, c->join_ev[s], 0);
   }
-  if (e == cudaSuccess) { e = k_symmetrize(c->d_M, c->d_G, n, cs); kernels++; }
+  if (e == cudaSuccess) {
+    e = k_symmetrize_blocks(c->d_M, c->d_G, c->d_mol_off, c->d_mol_n, c->nmol, c->total_elems, cs);
+    kernels++;
+  }
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(cs, &g);
   if (e == cudaSuccess) e = e2;
@@ -823,7 +883,7 @@ static int capture_jk_graph(fock_ctx* c) {
 
 int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
   if (!c || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
-  const size_t nn = (size_t)c->nbf * c->nbf;
+  const size_t nn = (size_t)c->total_elems;
   if (!c->jk_exec) {
     int rc = capture_jk_graph(c);
     if (rc != FOCK_OK) return rc;
@@ -1315,6 +1375,353 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   res->fock_seconds = fock_ms * 1e-3;
   res->fock_builds = builds;
   res->scf_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  cleanup();
+  if (fail != FOCK_OK) return fail;
+  return result;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batches: many molecules of uneven size solved together.  One context holds
+// all molecules (pairs and quartets never mix molecules); every class launch
+// of the captured Fock build covers the whole batch.  The SCF runs in lockstep
+// over molecules; molecules are ordered by (basis size, occupied orbitals) so
+// that runs of equal shape use strided-batched cuBLAS / cuSOLVER calls.
+// ---------------------------------------------------------------------------
+struct fock_batch {
+  fock_ctx* c = nullptr;
+  std::vector<int> perm;         // internal molecule -> caller's index
+  std::vector<int> mol_natom0;   // internal molecule -> first atom (internal)
+  std::vector<int> mol_natom;
+  std::vector<int> zsum;         // nuclear charge sum per internal molecule
+};
+
+extern "C" {
+
+int fock_batch_create(const fock_atom* atoms, const int* mol_atom_begin, const fock_shell* shells,
+                      const int* mol_shell_begin, int nmol, const fock_options* opt, fock_batch** out) {
+  if (!out || !atoms || !mol_atom_begin || !shells || !mol_shell_begin || nmol <= 0) return FOCK_ERR_INVALID_ARG;
+  *out = nullptr;
+  for (int m = 0; m < nmol; ++m)
+    if (mol_atom_begin[m + 1] <= mol_atom_begin[m] || mol_shell_begin[m + 1] <= mol_shell_begin[m])
+      return FOCK_ERR_INVALID_ARG;
+  // order molecules by (basis size, electrons)
+  std::vector<int> nbf(nmol, 0), zs(nmol, 0);
+  for (int m = 0; m < nmol; ++m) {
+    for (int s = mol_shell_begin[m]; s < mol_shell_begin[m + 1]; ++s) {
+      if (shells[s].atom < mol_atom_begin[m] || shells[s].atom >= mol_atom_begin[m + 1]) return FOCK_ERR_INVALID_ARG;
+      if (shells[s].l < 0 || shells[s].l > kMaxL) return FOCK_ERR_UNSUPPORTED_L;
+      nbf[m] += ncart(shells[s].l);
+    }
+    for (int a = mol_atom_begin[m]; a < mol_atom_begin[m + 1]; ++a) zs[m] += atoms[a].Z;
+  }
+  std::vector<int> perm(nmol);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(),
+                   [&](int x, int y) { return nbf[x] != nbf[y] ? nbf[x] < nbf[y] : zs[x] < zs[y]; });
+  std::vector<fock_atom> at;
+  std::vector<fock_shell> sh;
+  std::vector<int> sbeg{0};
+  fock_batch* b = new fock_batch();
+  for (int k = 0; k < nmol; ++k) {
+    const int m = perm[k];
+    const int a0 = (int)at.size();
+    b->mol_natom0.push_back(a0);
+    b->mol_natom.push_back(mol_atom_begin[m + 1] - mol_atom_begin[m]);
+    b->zsum.push_back(zs[m]);
+    for (int a = mol_atom_begin[m]; a < mol_atom_begin[m + 1]; ++a) at.push_back(atoms[a]);
+    for (int s = mol_shell_begin[m]; s < mol_shell_begin[m + 1]; ++s) {
+      fock_shell x = shells[s];
+      x.atom = a0 + (shells[s].atom - mol_atom_begin[m]);
+      sh.push_back(x);
+    }
+    sbeg.push_back((int)sh.size());
+  }
+  b->perm = perm;
+  const int rc = create_ctx(at.data(), (int)at.size(), sh.data(), (int)sh.size(), opt, sbeg.data(), nmol, &b->c);
+  if (rc != FOCK_OK) { delete b; return rc; }
+  *out = b;
+  return FOCK_OK;
+}
+
+void fock_batch_destroy(fock_batch* b) {
+  if (!b) return;
+  fock_ctx_destroy(b->c);
+  delete b;
+}
+
+int fock_batch_layout(const fock_batch* b, long long* offsets, int* nbf) {
+  if (!b) return FOCK_ERR_INVALID_ARG;
+  const fock_ctx* c = b->c;
+  for (int k = 0; k < c->nmol; ++k) {
+    if (offsets) offsets[b->perm[k]] = c->mol_off[k];
+    if (nbf) nbf[b->perm[k]] = c->mol_nbf[k];
+  }
+  return c->nmol;
+}
+
+int fock_batch_set_precision(fock_batch* b, int precision, double mixed_threshold) {
+  return b ? fock_set_precision(b->c, precision, mixed_threshold) : FOCK_ERR_INVALID_ARG;
+}
+
+int fock_batch_get_stats(const fock_batch* b, fock_stats* st) { return b ? fock_get_stats(b->c, st) : FOCK_ERR_INVALID_ARG; }
+
+int fock_batch_set_stream(fock_batch* b, void* stream) { return b ? fock_set_stream(b->c, stream) : FOCK_ERR_INVALID_ARG; }
+
+long long fock_batch_launch_count(const fock_batch* b) { return b ? b->c->launches : 0; }
+
+int fock_batch_build_jk_device(fock_batch* b, const double* D_dev, double* G_dev) {
+  return b ? fock_build_jk_device(b->c, D_dev, G_dev) : FOCK_ERR_INVALID_ARG;
+}
+
+// Lockstep RHF over the batch (try_scf per molecule, scf/src/lib.rs:73-258).
+// results[m] follows the caller's molecule order; its optional buffers are
+// ignored.  Every molecule stops updating its result at its own convergence
+// iteration; the loop ends when all have converged or max_iters is reached.
+int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) {
+  if (!b || !results) return FOCK_ERR_INVALID_ARG;
+  fock_ctx* c = b->c;
+  CK(cudaSetDevice(c->device));
+  auto t_start = std::chrono::steady_clock::now();
+  const int nmol = c->nmol;
+  const long long T = c->total_elems;
+  const bool refc = c->opt.eri_mode == FOCK_ERI_REFCOMPAT;
+  if (refc) return FOCK_ERR_INVALID_ARG;
+  int rc = ensure_blas(c);
+  if (rc != FOCK_OK) return rc;
+  cudaStream_t s = c->stream;
+  // electrons, nuclear repulsion, runs of equal (n, nocc)
+  std::vector<int> nocc(nmol), ne(nmol);
+  std::vector<double> vnn(nmol, 0.0);
+  for (int k = 0; k < nmol; ++k) {
+    const int q = charges ? charges[b->perm[k]] : 0;
+    ne[k] = b->zsum[k] - q;
+    if (ne[k] < 0 || ne[k] > 2 * c->mol_nbf[k]) return FOCK_ERR_INVALID_ARG;
+    nocc[k] = ne[k] / 2;
+    const int a0 = b->mol_natom0[k], na = b->mol_natom[k];
+    for (int i = a0; i < a0 + na; ++i)
+      for (int j = i + 1; j < a0 + na; ++j) {
+        const double dx = c->atoms[j].x - c->atoms[i].x, dy = c->atoms[j].y - c->atoms[i].y,
+                     dz = c->atoms[j].z - c->atoms[i].z;
+        vnn[k] += (double)c->atoms[i].Z * c->atoms[j].Z / std::sqrt(dx * dx + dy * dy + dz * dz);
+      }
+  }
+  struct Run { int m0, cnt, n, nocc; long long off, woff; };
+  std::vector<Run> runs;
+  std::vector<long long> woff(nmol + 1, 0);
+  for (int k = 0; k < nmol; ++k) woff[k + 1] = woff[k] + c->mol_nbf[k];
+  for (int k = 0; k < nmol;) {
+    int e = k + 1;
+    while (e < nmol && c->mol_nbf[e] == c->mol_nbf[k] && nocc[e] == nocc[k]) ++e;
+    runs.push_back({k, e - k, c->mol_nbf[k], nocc[k], c->mol_off[k], woff[k]});
+    k = e;
+  }
+  const int ring = std::max(1, std::min(c->opt.diis_len, 16));
+  std::vector<void*> bufs;
+  bool ok = true;
+  auto mk = [&](size_t bytes) -> void* {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 8)) != cudaSuccess) { ok = false; return nullptr; }
+    bufs.push_back(p);
+    return p;
+  };
+  const size_t TB = (size_t)T * 8;
+  double *S = (double*)mk(TB), *Tk = (double*)mk(TB), *V = (double*)mk(TB), *H = (double*)mk(TB);
+  double *X = (double*)mk(TB), *W = (double*)mk(TB), *U = (double*)mk(TB), *w = (double*)mk(woff[nmol] * 8);
+  double *F = (double*)mk(TB), *Fd = (double*)mk(TB), *G = (double*)mk(TB), *Dm = (double*)mk(TB);
+  double *Dn = (double*)mk(TB), *Cm = (double*)mk(TB), *T1 = (double*)mk(TB), *T2 = (double*)mk(TB);
+  double *Fring = (double*)mk(TB * ring), *Ering = (double*)mk(TB * ring);
+  double* Bm = (double*)mk((size_t)nmol * ring * ring * 8);
+  double* coef = (double*)mk((size_t)nmol * (ring + 1) * 8);
+  double* ecur = (double*)mk((size_t)nmol * 8);
+  double* eref = (double*)mk((size_t)nmol * 8);
+  unsigned long long* errb = (unsigned long long*)mk((size_t)nmol * 8);
+  int* d_order = (int*)mk(ring * sizeof(int));
+  int* d_info = (int*)mk((size_t)nmol * sizeof(int));
+  long long* d_woff = (long long*)mk((nmol + 1) * sizeof(long long));
+  auto cleanup = [&]() { for (void* p : bufs) cudaFree(p); };
+  if (!ok) { cleanup(); return FOCK_ERR_OOM; }
+  int fail = FOCK_OK;
+  auto cku = [&](cudaError_t x) { if (x != cudaSuccess && fail == FOCK_OK) fail = map_cuda(x); };
+  auto ckb = [&](cublasStatus_t x) { if (x != CUBLAS_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
+  auto cks = [&](cusolverStatus_t x) { if (x != CUSOLVER_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
+  cku(cudaMemcpyAsync(d_woff, woff.data(), (nmol + 1) * sizeof(long long), cudaMemcpyHostToDevice, s));
+  // one-electron matrices per molecule (textbook convention)
+  for (int k = 0; k < nmol && fail == FOCK_OK; ++k) {
+    MdBasis mb = md_basis(c);
+    mb.funcs = c->d_mdfuncs + c->mol_f0[k];
+    mb.nfunc = c->mol_nbf[k];
+    const long long o = c->mol_off[k];
+    cku(md_one_electron(mb, md_tables(c), c->d_atoms4 + 4 * b->mol_natom0[k], b->mol_natom[k], 0, S + o, Tk + o, V + o,
+                        s));
+    c->launches++;
+  }
+  cku(k_add(Tk, V, H, (int)T, s));
+  c->launches++;
+  // batched dense algebra per run
+  const double one = 1.0, zero = 0.0, two = 2.0;
+  auto gemm = [&](const Run& r, cublasOperation_t ta, cublasOperation_t tb, int kdim, const double* alpha,
+                  const double* A, const double* Bq, double* Cc) {
+    const long long st = (long long)r.n * r.n;
+    ckb(cublasDgemmStridedBatched(c->blas, ta, tb, r.n, r.n, kdim, alpha, A + r.off, r.n, st, Bq + r.off, r.n, st,
+                                  &zero, Cc + r.off, r.n, st, r.cnt));
+    c->launches++;
+  };
+  cusolverDnParams_t sp = nullptr;
+  cks(cusolverDnCreateParams(&sp));
+  size_t dws = 0, hws = 0;
+  for (const Run& r : runs) {
+    size_t d1 = 0, h1 = 0;
+    cks(cusolverDnXsyevBatched_bufferSize(c->solver, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r.n,
+                                          CUDA_R_64F, U + r.off, r.n, CUDA_R_64F, w + r.woff, CUDA_R_64F, &d1, &h1,
+                                          r.cnt));
+    dws = std::max(dws, d1);
+    hws = std::max(hws, h1);
+  }
+  void* dwork = mk(dws);
+  std::vector<char> hwork(std::max<size_t>(hws, 8));
+  if (!ok) { if (sp) cusolverDnDestroyParams(sp); cleanup(); return FOCK_ERR_OOM; }
+  auto syev = [&](double* A) {  // eigenvectors in place, eigenvalues into w
+    for (const Run& r : runs) {
+      cks(cusolverDnXsyevBatched(c->solver, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r.n, CUDA_R_64F,
+                                 A + r.off, r.n, CUDA_R_64F, w + r.woff, CUDA_R_64F, dwork, dws, hwork.data(), hws,
+                                 d_info + r.m0, r.cnt));
+      c->launches++;
+    }
+  };
+  // Loewdin X = U diag(w^-1/2) U^T
+  cku(cudaMemcpyAsync(U, S, TB, cudaMemcpyDeviceToDevice, s));
+  syev(U);
+  cku(kb_scale_cols(U, w, d_woff, c->d_mol_off, c->d_mol_n, nmol, T, W, s));
+  c->launches++;
+  for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.n, &one, W, U, X);
+  auto density_from = [&](const double* Fin, double* Dout) {
+    for (const Run& r : runs) gemm(r, CUBLAS_OP_T, CUBLAS_OP_N, r.n, &one, X, Fin, T1);
+    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, X, T2);
+    syev(T2);
+    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T2, Cm);
+    for (const Run& r : runs) {
+      if (r.nocc > 0) {
+        gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.nocc, &two, Cm, Cm, Dout);
+      } else {
+        cku(cudaMemsetAsync(Dout + r.off, 0, (size_t)r.cnt * r.n * r.n * 8, s));
+      }
+    }
+  };
+  cku(kb_guess(S, H, c->d_mol_off, c->d_mol_n, nmol, T, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, F, s));
+  c->launches++;
+  density_from(F, Dm);
+
+  const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
+  const double mixed_th = c->opt.mixed_threshold;
+  bool fp64_phase = !mixed;
+  std::vector<int> done(nmol, 0);
+  std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol);
+  std::vector<unsigned long long> hb(nmol);
+  for (int k = 0; k < nmol; ++k) {
+    fock_scf_result& o = results[b->perm[k]];
+    o.converged = 0;
+    o.n_basis = c->mol_nbf[k];
+    o.n_electrons = ne[k];
+    o.nuclear_repulsion = vnn[k];
+  }
+  std::vector<int> order;
+  int next_slot = 0, builds = 0, ndone = 0, it_last = 0;
+  double fock_ms = 0.0;
+  cudaEvent_t ev0, ev1;
+  cudaEventCreate(&ev0);
+  cudaEventCreate(&ev1);
+  int result = FOCK_OK;
+  for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
+    it_last = iter;
+    cudaEventRecord(ev0, s);
+    { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
+    cudaEventRecord(ev1, s);
+    builds++;
+    cku(k_add(H, G, F, (int)T, s));
+    cku(kb_energy(Dm, H, G, c->d_mol_off, nmol, ecur, s));
+    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, F, Dm, T1);
+    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
+    const int slot = next_slot;
+    next_slot = (next_slot + 1) % ring;
+    if ((int)order.size() == ring) order.erase(order.begin());
+    order.push_back(slot);
+    cku(kb_commutator(T2, Ering + (size_t)slot * T, c->d_mol_off, c->d_mol_n, nmol, errb, s));
+    cku(cudaMemcpyAsync(Fring + (size_t)slot * T, F, TB, cudaMemcpyDeviceToDevice, s));
+    const int nused = (int)order.size();
+    cku(kb_diis_dots(Ering, T, slot, nused, ring, c->d_mol_off, nmol, Bm, s));
+    c->launches += 4;
+    const double* Fuse = F;
+    if (nused >= c->opt.diis_start) {
+      cku(cudaMemcpyAsync(d_order, order.data(), nused * sizeof(int), cudaMemcpyHostToDevice, s));
+      cku(kb_diis_solve(Bm, ring, d_order, nused, coef, nmol, s));
+      cku(kb_diis_extrapolate(Fring, T, d_order, nused, coef, ring, slot, c->d_mol_off, nmol, Fd, s));
+      c->launches += 2;
+      Fuse = Fd;
+    }
+    density_from(Fuse, Dn);
+    cku(kb_energy(Dn, H, G, c->d_mol_off, nmol, eref, s));
+    c->launches++;
+    cku(cudaMemcpyAsync(he.data(), ecur, nmol * 8, cudaMemcpyDeviceToHost, s));
+    cku(cudaMemcpyAsync(hr.data(), eref, nmol * 8, cudaMemcpyDeviceToHost, s));
+    cku(cudaMemcpyAsync(hb.data(), errb, nmol * 8, cudaMemcpyDeviceToHost, s));
+    cku(cudaStreamSynchronize(s));
+    if (fail != FOCK_OK) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ev0, ev1);
+    fock_ms += ms;
+    double maxerr = 0.0;
+    bool diverged = false;
+    for (int k = 0; k < nmol; ++k) {
+      std::memcpy(&errv[k], &hb[k], 8);
+      if (!done[k]) maxerr = std::max(maxerr, errv[k]);
+      if (!done[k] && !std::isfinite(errv[k])) diverged = true;
+    }
+    if (diverged) { result = FOCK_ERR_DIVERGED; break; }
+    if (!fp64_phase && (maxerr < kMixedSwitch || iter >= c->opt.max_iters / 2)) {
+      // all molecules close to convergence: finish in FP64
+      int r = fock_set_precision(c, FOCK_PREC_FP64, mixed_th);
+      if (r != FOCK_OK) { fail = r; break; }
+      fp64_phase = true;
+      for (int k = 0; k < nmol; ++k) eprev[k] = he[k];
+      std::swap(Dm, Dn);
+      continue;
+    }
+    if (fp64_phase) {
+      for (int k = 0; k < nmol; ++k) {
+        if (done[k]) continue;
+        bool conv;
+        if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) conv = errv[k] < c->opt.epsilon;
+        else conv = iter > 0 && std::fabs(he[k] - eprev[k]) < c->opt.epsilon && errv[k] < std::sqrt(c->opt.epsilon);
+        if (conv || iter == c->opt.max_iters) {
+          fock_scf_result& o = results[b->perm[k]];
+          const double e = c->opt.energy_mode == 0 ? hr[k] : he[k];
+          o.electronic_energy = e;
+          o.total_energy = e + vnn[k];
+          o.iterations = iter;
+          o.converged = conv ? 1 : 0;
+          done[k] = 1;
+          ++ndone;
+        }
+      }
+      if (ndone == nmol) break;
+    }
+    for (int k = 0; k < nmol; ++k) eprev[k] = he[k];
+    std::swap(Dm, Dn);
+  }
+  (void)it_last;
+  if (mixed && fp64_phase) fock_set_precision(c, FOCK_PREC_MIXED, mixed_th);
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  if (sp) cusolverDnDestroyParams(sp);
+  const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  for (int k = 0; k < nmol; ++k) {
+    fock_scf_result& o = results[b->perm[k]];
+    o.scf_seconds = wall;
+    o.fock_seconds = fock_ms * 1e-3;
+    o.fock_builds = builds;
+  }
   cleanup();
   if (fail != FOCK_OK) return fail;
   return result;

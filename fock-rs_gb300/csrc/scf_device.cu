@@ -23,6 +23,23 @@ __global__ void symmetrize_kernel(const double* M, double* G, int n) {
   G[t] = M[(size_t)i * n + j] + M[(size_t)j * n + i];
 }
 
+// Block-wise G = M + M^T over molecule blocks [off[m], off[m+1]) of size
+// n[m] x n[m] (row-major).
+__global__ void symmetrize_blocks_kernel(const double* M, double* G, const long long* __restrict__ off,
+                                         const int* __restrict__ n, int nmol, long long total) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  const long long loc = t - off[lo];
+  const int nm = n[lo];
+  const int i = (int)(loc / nm), j = (int)(loc % nm);
+  G[t] = M[t] + M[off[lo] + (long long)j * nm + i];
+}
+
 __global__ void to_float_kernel(const double* a, float* b, int nn) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < nn) b[t] = (float)a[t];
@@ -178,6 +195,11 @@ cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s) {
   symmetrize_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(M, G, n);
   return cudaGetLastError();
 }
+cudaError_t k_symmetrize_blocks(const double* M, double* G, const long long* off, const int* n, int nmol,
+                                long long total, cudaStream_t s) {
+  symmetrize_blocks_kernel<<<blocks_for(total, 256), 256, 0, s>>>(M, G, off, n, nmol, total);
+  return cudaGetLastError();
+}
 cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s) {
   to_float_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, nn);
   return cudaGetLastError();
@@ -230,6 +252,212 @@ cudaError_t fma_peak(int fp64, int blocks, int threads, int iters, void* out, fl
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+}  // namespace fockgb
+
+// ---------------------------------------------------------------------------
+// Batched (per molecule block) variants.  Molecule m owns the n[m] x n[m]
+// column-major block [off[m], off[m+1]) of every matrix array.
+// ---------------------------------------------------------------------------
+namespace fockgb {
+
+__device__ __forceinline__ int block_of(const long long* off, int nmol, long long t) {
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// out[m] = 1/2 sum D (2H + G) over block m; one block of threads per molecule.
+__global__ void energy_blocks_kernel(const double* D, const double* H, const double* G, const long long* off,
+                                     int nmol, double* out) {
+  const int m = blockIdx.x;
+  if (m >= nmol) return;
+  double acc = 0.0;
+  for (long long t = off[m] + threadIdx.x; t < off[m + 1]; t += blockDim.x) acc += 0.5 * D[t] * (2.0 * H[t] + G[t]);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sm[i];
+    out[m] = s;
+  }
+}
+
+// E = A - A^T per block and errmax[m] = max |E| (bit pattern of a non-negative double).
+__global__ void commutator_blocks_kernel(const double* A, double* E, const long long* off, const int* n, int nmol,
+                                         unsigned long long* errbits) {
+  const int m = blockIdx.x;
+  if (m >= nmol) return;
+  const int nm = n[m];
+  const long long o = off[m];
+  double mx = 0.0;
+  for (int t = threadIdx.x; t < nm * nm; t += blockDim.x) {
+    const int r = t % nm, c = t / nm;
+    const double v = A[o + t] - A[o + (long long)r * nm + c];
+    E[o + t] = v;
+    mx = fmax(mx, isnan(v) ? INFINITY : fabs(v));
+  }
+  for (int s = 16; s > 0; s >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, s));
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double r = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r = fmax(r, sm[i]);
+    errbits[m] = (unsigned long long)__double_as_longlong(r);
+  }
+}
+
+// B[m][slot][k] = B[m][k][slot] = <E_slot, E_k>_m for k < nused; grid (nmol, nused).
+__global__ void diis_dots_blocks_kernel(const double* Ering, long long total, int slot, int ring,
+                                        const long long* off, int nmol, double* B) {
+  const int m = blockIdx.x, k = blockIdx.y;
+  if (m >= nmol) return;
+  const double* a = Ering + (long long)slot * total;
+  const double* b = Ering + (long long)k * total;
+  double acc = 0.0;
+  for (long long t = off[m] + threadIdx.x; t < off[m + 1]; t += blockDim.x) acc += a[t] * b[t];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sm[i];
+    double* Bm = B + (long long)m * ring * ring;
+    Bm[slot * ring + k] = s;
+    Bm[k * ring + slot] = s;
+  }
+}
+
+// Pulay DIIS per molecule (one thread each): solve [B -1; -1 0] c = [0; -1]
+// over the slots order[0..mu) by Gaussian elimination with partial pivoting.
+__global__ void diis_solve_blocks_kernel(const double* B, int ring, const int* order, int mu, double* coef,
+                                         int nmol) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= nmol) return;
+  const double* Bm = B + (long long)m * ring * ring;
+  double* cm = coef + (long long)m * (ring + 1);
+  double A[17 * 17], rhs[17];
+  const int M = mu + 1;
+  for (int i = 0; i < mu; ++i) {
+    for (int j = 0; j < mu; ++j) A[i * M + j] = Bm[order[i] * ring + order[j]];
+    A[i * M + mu] = -1.0;
+    A[mu * M + i] = -1.0;
+    rhs[i] = 0.0;
+  }
+  A[mu * M + mu] = 0.0;
+  rhs[mu] = -1.0;
+  bool ok = true;
+  for (int c = 0; c < M && ok; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < M; ++r)
+      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
+    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
+    if (piv != c) {
+      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
+      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
+    }
+    for (int r = c + 1; r < M; ++r) {
+      const double f = A[r * M + c] / A[c * M + c];
+      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
+      rhs[r] -= f * rhs[c];
+    }
+  }
+  if (ok) {
+    for (int c = M - 1; c >= 0; --c) {
+      double s = rhs[c];
+      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
+      rhs[c] = s / A[c * M + c];
+      if (!isfinite(rhs[c])) ok = false;
+    }
+  }
+  for (int i = 0; i < mu; ++i) cm[i] = ok ? rhs[i] : 0.0;
+  cm[ring] = ok ? 1.0 : 0.0;
+}
+
+__global__ void diis_extrapolate_blocks_kernel(const double* Fring, long long total, const int* order, int mu,
+                                               const double* coef, int ring, int last, const long long* off,
+                                               int nmol, double* Fd) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int m = block_of(off, nmol, t);
+  const double* cm = coef + (long long)m * (ring + 1);
+  if (cm[ring] == 0.0) { Fd[t] = Fring[(long long)last * total + t]; return; }
+  double acc = 0.0;
+  for (int i = 0; i < mu; ++i) acc += cm[i] * Fring[(long long)order[i] * total + t];
+  Fd[t] = acc;
+}
+
+// W = U diag(w^{-1/2}) per block (column scaling); w packed per molecule at woff[m].
+__global__ void scale_cols_blocks_kernel(const double* U, const double* w, const long long* woff,
+                                         const long long* off, const int* n, int nmol, long long total, double* W) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  const int m = block_of(off, nmol, t);
+  const int col = (int)((t - off[m]) / n[m]);
+  W[t] = U[t] / sqrt(w[woff[m] + col]);
+}
+
+// GWH guess 0.875 S_ij (H_ii + H_jj) or F = H, per block.
+__global__ void guess_blocks_kernel(const double* S, const double* H, const long long* off, const int* n, int nmol,
+                                    long long total, int gwh, double* F) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  if (!gwh) { F[t] = H[t]; return; }
+  const int m = block_of(off, nmol, t);
+  const int nm = n[m];
+  const long long loc = t - off[m];
+  const int i = (int)(loc % nm), j = (int)(loc / nm);
+  F[t] = 0.875 * S[t] * (H[off[m] + (long long)i * nm + i] + H[off[m] + (long long)j * nm + j]);
+}
+
+static unsigned nblk(long long n, int thr) { return (unsigned)((n + thr - 1) / thr); }
+
+cudaError_t kb_energy(const double* D, const double* H, const double* G, const long long* off, int nmol, double* out,
+                      cudaStream_t s) {
+  energy_blocks_kernel<<<nmol, 256, 0, s>>>(D, H, G, off, nmol, out);
+  return cudaGetLastError();
+}
+cudaError_t kb_commutator(const double* A, double* E, const long long* off, const int* n, int nmol,
+                          unsigned long long* errbits, cudaStream_t s) {
+  commutator_blocks_kernel<<<nmol, 256, 0, s>>>(A, E, off, n, nmol, errbits);
+  return cudaGetLastError();
+}
+cudaError_t kb_diis_dots(const double* Ering, long long total, int slot, int nused, int ring, const long long* off,
+                         int nmol, double* B, cudaStream_t s) {
+  diis_dots_blocks_kernel<<<dim3(nmol, nused), 256, 0, s>>>(Ering, total, slot, ring, off, nmol, B);
+  return cudaGetLastError();
+}
+cudaError_t kb_diis_solve(const double* B, int ring, const int* order, int mu, double* coef, int nmol,
+                          cudaStream_t s) {
+  diis_solve_blocks_kernel<<<nblk(nmol, 32), 32, 0, s>>>(B, ring, order, mu, coef, nmol);
+  return cudaGetLastError();
+}
+cudaError_t kb_diis_extrapolate(const double* Fring, long long total, const int* order, int mu, const double* coef,
+                                int ring, int last, const long long* off, int nmol, double* Fd, cudaStream_t s) {
+  diis_extrapolate_blocks_kernel<<<nblk(total, 256), 256, 0, s>>>(Fring, total, order, mu, coef, ring, last, off,
+                                                                  nmol, Fd);
+  return cudaGetLastError();
+}
+cudaError_t kb_scale_cols(const double* U, const double* w, const long long* woff, const long long* off,
+                          const int* n, int nmol, long long total, double* W, cudaStream_t s) {
+  scale_cols_blocks_kernel<<<nblk(total, 256), 256, 0, s>>>(U, w, woff, off, n, nmol, total, W);
+  return cudaGetLastError();
+}
+cudaError_t kb_guess(const double* S, const double* H, const long long* off, const int* n, int nmol, long long total,
+                     int gwh, double* F, cudaStream_t s) {
+  guess_blocks_kernel<<<nblk(total, 256), 256, 0, s>>>(S, H, off, n, nmol, total, gwh, F);
   return cudaGetLastError();
 }
 

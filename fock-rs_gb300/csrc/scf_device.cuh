@@ -5,6 +5,8 @@
 namespace fockgb {
 cudaError_t k_add(const double* a, const double* b, double* c, int nn, cudaStream_t s);
 cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s);
+cudaError_t k_symmetrize_blocks(const double* M, double* G, const long long* off, const int* n, int nmol,
+                                long long total, cudaStream_t s);
 cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s);
 cudaError_t k_guess(const double* S, const double* H, double* F, int n, int gwh, cudaStream_t s);
 cudaError_t k_scale_cols(const double* U, const double* w, double* W, int n, cudaStream_t s);
@@ -15,4 +17,22 @@ cudaError_t k_diis_solve(const double* B, int ring, const int* order, int m, dou
 cudaError_t k_diis_extrapolate(const double* Fring, int nn, const int* order, int m, const double* coef, int last,
                                double* Fd, cudaStream_t s);
 cudaError_t fma_peak(int fp64, int blocks, int threads, int iters, void* out, float* ms);
+}  // namespace fockgb
+
+namespace fockgb {
+// batched (per molecule block) kernels, see scf_device.cu
+cudaError_t kb_energy(const double* D, const double* H, const double* G, const long long* off, int nmol, double* out,
+                      cudaStream_t s);
+cudaError_t kb_commutator(const double* A, double* E, const long long* off, const int* n, int nmol,
+                          unsigned long long* errbits, cudaStream_t s);
+cudaError_t kb_diis_dots(const double* Ering, long long total, int slot, int nused, int ring, const long long* off,
+                         int nmol, double* B, cudaStream_t s);
+cudaError_t kb_diis_solve(const double* B, int ring, const int* order, int mu, double* coef, int nmol,
+                          cudaStream_t s);
+cudaError_t kb_diis_extrapolate(const double* Fring, long long total, const int* order, int mu, const double* coef,
+                                int ring, int last, const long long* off, int nmol, double* Fd, cudaStream_t s);
+cudaError_t kb_scale_cols(const double* U, const double* w, const long long* woff, const long long* off,
+                          const int* n, int nmol, long long total, double* W, cudaStream_t s);
+cudaError_t kb_guess(const double* S, const double* H, const long long* off, const int* n, int nmol, long long total,
+                     int gwh, double* F, cudaStream_t s);
 }  // namespace fockgb

@@ -141,6 +141,86 @@ class FockContext:
         return g.reshape(-1, 3)
 
 
+class FockBatch:
+    """Many molecules solved together (fock_batch_*): one context, class
+    launches over the whole batch, lockstep SCF with batched dense algebra."""
+
+    def __init__(self, molecules: Sequence[Sequence[Atom]], opts: Optional[_lib.Options] = None, **kw):
+        self.molecules = [list(m) for m in molecules]
+        self.opts = opts if opts is not None else options(**kw)
+        atoms, shells, abeg, sbeg = [], [], [0], [0]
+        self._keep = []
+        for mol in self.molecules:
+            base = len(atoms)
+            for a in mol:
+                atoms.append(_lib.Atom(float(a.position[0]), float(a.position[1]), float(a.position[2]), int(a.Z)))
+            for s in shells_of(mol):
+                e = np.ascontiguousarray(s.exps, dtype=np.float64)
+                c = np.ascontiguousarray(s.coefs, dtype=np.float64)
+                self._keep += [e, c]
+                shells.append(_lib.Shell(int(s.l), len(e), base + int(s.atom), _dp(e), _dp(c)))
+            abeg.append(len(atoms))
+            sbeg.append(len(shells))
+        catoms = (_lib.Atom * len(atoms))(*atoms)
+        cshells = (_lib.Shell * len(shells))(*shells)
+        cab = (C.c_int * len(abeg))(*abeg)
+        csb = (C.c_int * len(sbeg))(*sbeg)
+        self._keep += [catoms, cshells, cab, csb]
+        h = C.c_void_p()
+        check(lib().fock_batch_create(catoms, cab, cshells, csb, len(self.molecules), C.byref(self.opts),
+                                      C.byref(h)), "fock_batch_create")
+        self.handle = h
+        n = len(self.molecules)
+        off = (C.c_longlong * n)()
+        nbf = (C.c_int * n)()
+        lib().fock_batch_layout(h, off, nbf)
+        self.offsets = list(off)
+        self.nbf = list(nbf)
+        self.total = max(o + b * b for o, b in zip(self.offsets, self.nbf))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().fock_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_precision(self, precision, mixed_threshold=1.0):
+        check(lib().fock_batch_set_precision(self.handle, precision, mixed_threshold), "fock_batch_set_precision")
+
+    def set_stream(self, stream_ptr: int):
+        check(lib().fock_batch_set_stream(self.handle, C.c_void_p(stream_ptr or None)), "fock_batch_set_stream")
+
+    def stats(self) -> dict:
+        st = _lib.Stats()
+        check(lib().fock_batch_get_stats(self.handle, C.byref(st)), "fock_batch_get_stats")
+        return {k: getattr(st, k) for k, _ in _lib.Stats._fields_}
+
+    def launch_count(self) -> int:
+        return lib().fock_batch_launch_count(self.handle)
+
+    def build_jk_device(self, d_ptr: int, g_ptr: int):
+        check(lib().fock_batch_build_jk_device(self.handle, C.c_void_p(d_ptr), C.c_void_p(g_ptr)),
+              "fock_batch_build_jk_device")
+
+    def scf(self, charges=None):
+        n = len(self.molecules)
+        res = (_lib.ScfResult * n)()
+        ch = (C.c_int * n)(*(charges or [0] * n)) if charges is not None else None
+        rc = lib().fock_batch_scf(self.handle, ch, res)
+        return rc, [res[i] for i in range(n)]
+
+
 class ElectronTensor:
     """ElectronTensor::from_basis (basis/src/electron_tensor.rs:81): full N^4
     tensor computed on the GPU, indexed in chemists' notation (ij|kl)."""

@@ -85,6 +85,19 @@ def lib():
         L.fock_one_electron.argtypes = [vp, dp, dp, dp]
         L.fock_scf.argtypes = [vp, C.c_int, C.POINTER(ScfResult)]
         L.fock_set_stream.argtypes = [vp, vp]
+        ip = C.POINTER(C.c_int)
+        L.fock_batch_create.argtypes = [C.POINTER(Atom), ip, C.POINTER(Shell), ip, C.c_int, C.POINTER(Options),
+                                        C.POINTER(vp)]
+        L.fock_batch_destroy.argtypes = [vp]
+        L.fock_batch_destroy.restype = None
+        L.fock_batch_layout.argtypes = [vp, C.POINTER(C.c_longlong), ip]
+        L.fock_batch_set_precision.argtypes = [vp, C.c_int, C.c_double]
+        L.fock_batch_get_stats.argtypes = [vp, C.POINTER(Stats)]
+        L.fock_batch_set_stream.argtypes = [vp, vp]
+        L.fock_batch_launch_count.argtypes = [vp]
+        L.fock_batch_launch_count.restype = C.c_longlong
+        L.fock_batch_build_jk_device.argtypes = [vp, vp, vp]
+        L.fock_batch_scf.argtypes = [vp, ip, C.POINTER(ScfResult)]
         L.fock_gradient.argtypes = [vp, dp, dp, dp]
         L.fock_energy_backward.argtypes = [vp, C.POINTER(ScfResult), dp]
         L.fock_launch_count.argtypes = [vp]

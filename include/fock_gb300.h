@@ -217,6 +217,30 @@ typedef struct {
 } fock_launch_profile;
 int fock_profile_build(fock_ctx* ctx, const double* D_dev, fock_launch_profile* out, int cap);
 
+/* ---- batches: many molecules of uneven size solved together ----
+ * (no counterpart in the reference, which solves one molecule per try_scf).
+ * Molecule m owns atoms [mol_atom_begin[m], mol_atom_begin[m+1]) and shells
+ * [mol_shell_begin[m], mol_shell_begin[m+1]); shell atom indices are global.
+ * Internally one context holds every molecule; each class launch of the
+ * captured Fock build covers the whole batch, and the SCF runs in lockstep
+ * with strided-batched dense algebra per run of equal-size molecules. */
+typedef struct fock_batch fock_batch;
+int fock_batch_create(const fock_atom* atoms, const int* mol_atom_begin, const fock_shell* shells,
+                      const int* mol_shell_begin, int nmol, const fock_options* opt, fock_batch** out);
+void fock_batch_destroy(fock_batch* batch);
+/* offsets[m] of molecule m's n_m x n_m block in the packed D / G arrays of
+ * fock_batch_build_jk_device, and n_m; returns the number of molecules. */
+int fock_batch_layout(const fock_batch* batch, long long* offsets, int* nbf);
+int fock_batch_set_precision(fock_batch* batch, int precision, double mixed_threshold);
+int fock_batch_get_stats(const fock_batch* batch, fock_stats* st);
+int fock_batch_set_stream(fock_batch* batch, void* stream);
+long long fock_batch_launch_count(const fock_batch* batch);
+/* G = J - K/2 for every molecule, packed blocks (textbook sign convention). */
+int fock_batch_build_jk_device(fock_batch* batch, const double* D_dev, double* G_dev);
+/* RHF of every molecule; charges may be NULL (neutral); results[nmol] in the
+ * caller's order (energies, iterations, convergence; buffers not filled). */
+int fock_batch_scf(fock_batch* batch, const int* charges, fock_scf_result* results);
+
 const char* fock_strerror(int code);
 
 /* FP64 / FP32 FMA-pipe throughput microbenchmark on this device: fills
