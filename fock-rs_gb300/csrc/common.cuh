@@ -84,6 +84,9 @@ struct ClassLaunch {
   const long long* row_off;
   int nrows;
   long long nlanes;
+  int block;                     // threads per block (0: default)
+  int persist_blocks;            // > 0: persistent launch with this many blocks
+  unsigned long long* queue;     // work-queue counter of the persistent launch
 };
 
 struct EriArgs {

@@ -22,7 +22,8 @@
 
 namespace fockgb {
 
-constexpr int kEriThreads = 128;
+constexpr int kEriThreads = 128;     // default block size (tunable per launch: 64..256)
+constexpr int kEriMaxThreads = 256;
 
 // unroll factor of the ket primitive loop (independent iterations interleave:
 // instruction-level parallelism for the long FP64 dependency chains)
@@ -118,24 +119,21 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
   ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
 }
 
+// The work of lane t of a launch (one contracted quartet, one bra slice).
 template <class C, typename R, int MODE>
-__global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, const EriArgs a) {
+__device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a, long long t) {
   constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, NE = C::NE, NF = C::NF, L = C::L;
-  const int lane = threadIdx.x & 31;
   int bra, ket;
   bool active;
   int slice = 0, nslice = 1;
   if (MODE == MODE_SCHWARZ) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
   } else {
-    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
     decode_lane(cl, t, bra, ket, slice, nslice);
     active = true;
   }
-  (void)lane;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
   // this warp's slice of the bra primitive pairs
@@ -307,6 +305,28 @@ __global__ void __launch_bounds__(kEriThreads) eri_kernel(const ClassLaunch cl, 
   }
 }
 
+template <class C, typename R, int MODE>
+__global__ void __launch_bounds__(kEriMaxThreads) eri_kernel(const ClassLaunch cl, const EriArgs a) {
+  eri_lane<C, R, MODE>(cl, a, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// Persistent variant: a grid sized to part of the GPU; every warp takes the
+// next 32 lanes of the launch from the launch's work queue (an atomic counter
+// cleared before every build) until the queue is empty.
+template <class C, typename R>
+__global__ void __launch_bounds__(kEriMaxThreads) eri_kernel_persistent(const ClassLaunch cl, const EriArgs a) {
+  const int lane = threadIdx.x & 31;
+  const long long nchunks = (cl.nlanes + 31) >> 5;
+  for (;;) {
+    unsigned long long chunk = 0;
+    if (lane == 0) chunk = atomicAdd(cl.queue, 1ULL);
+    chunk = __shfl_sync(0xffffffffu, chunk, 0);
+    if ((long long)chunk >= nchunks) break;
+    eri_lane<C, R, MODE_JK>(cl, a, (long long)chunk * 32 + lane);
+    __syncwarp();
+  }
+}
+
 // Nuclear gradient of the two-electron energy, fused: derivative integrals
 // (a+1_i b|cd), (a-1_i b|cd), ... are built per contracted quartet from
 // weighted primitive accumulators (2 alpha, 2 beta, 2 gamma, 1) and
@@ -425,14 +445,33 @@ cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int 
     }
   }
   if (cl.nlanes <= 0) return cudaSuccess;
-  const long long blocks = (cl.nlanes + kEriThreads - 1) / kEriThreads;
+  const int thr = (cl.block >= 32 && cl.block <= kEriMaxThreads) ? cl.block : kEriThreads;
+  const long long blocks = (cl.nlanes + thr - 1) / thr;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   if (mode == MODE_TENSOR) {
-    eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+    eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
+  } else if (cl.queue && cl.persist_blocks != 0) {
+    // persistent: half of the resident capacity of the GPU (other classes run
+    // beside it on the other streams of the captured build)
+    long long pb = cl.persist_blocks;
+    if (pb < 0) {
+      int dev = 0, nsm = 0, per_sm = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      if (prec == PREC_FP32)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eri_kernel_persistent<C, float>, thr, 0);
+      else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, eri_kernel_persistent<C, double>, thr, 0);
+      pb = (long long)(per_sm > 0 ? per_sm : 1) * (nsm > 0 ? nsm : 1) / 2;
+      if (pb < 1) pb = 1;
+    }
+    if (pb > blocks) pb = blocks;
+    if (prec == PREC_FP32) eri_kernel_persistent<C, float><<<(unsigned)pb, thr, 0, s>>>(cl, a);
+    else eri_kernel_persistent<C, double><<<(unsigned)pb, thr, 0, s>>>(cl, a);
   } else if (prec == PREC_FP32) {
-    eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+    eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   } else {
-    eri_kernel<C, double, MODE_JK><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+    eri_kernel<C, double, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   }
   return cudaGetLastError();
 }

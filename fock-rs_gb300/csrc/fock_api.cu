@@ -177,6 +177,7 @@ struct fock_ctx {
   // plans
   std::vector<Plan> plans;
   int* d_plan_int = nullptr;
+  size_t queue_base = 0;  // first work-queue counter in d_plan_ll
   long long* d_plan_ll = nullptr;
   fock_stats stats{};
   // molecules (one for fock_ctx_create, many for a batch)
@@ -417,6 +418,9 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     }
   }
   st.shell_quartets_screened = total_shell_quartets - st.shell_quartets_fp64 - st.shell_quartets_fp32;
+  // work-queue counters of persistent launches live after the row offsets
+  c->queue_base = lls.size();
+  lls.insert(lls.end(), pend.size() + 1, 0LL);
   CK(dalloc(&c->d_plan_int, ints.size()));
   CK(dalloc(&c->d_plan_ll, lls.size()));
   if (!ints.empty()) CK(cudaMemcpy(c->d_plan_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -428,6 +432,9 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.row_cnt = c->d_plan_int + P.cnt;
     P.p.cl.row_slices = c->d_plan_int + P.sl;
     P.p.cl.row_off = c->d_plan_ll + P.off;
+    P.p.cl.block = c->opt.block_threads;
+    P.p.cl.persist_blocks = (!for_tensor && c->opt.persistent) ? -1 : 0;
+    P.p.cl.queue = reinterpret_cast<unsigned long long*>(c->d_plan_ll + c->queue_base + c->plans.size());
     c->plans.push_back(P.p);
   }
   st.launches_per_build = (int)c->plans.size() + 1;
@@ -526,6 +533,8 @@ void fock_options_default(fock_options* o) {
   o->final_fp64 = 1;
   o->prims_per_slice = 1;
   o->prims_per_slice_fp32 = 4;
+  o->block_threads = 128;
+  o->persistent = 0;
   o->device = 0;
 }
 
@@ -856,6 +865,8 @@ static int capture_jk_graph(fock_ctx* c) {
   cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
   int kernels = 0;
   if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); kernels++; }
+  if (e == cudaSuccess && c->opt.persistent)
+    e = cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, (c->plans.size() + 1) * sizeof(long long), cs);
   if (e == cudaSuccess) e = cudaEventRecord(c->fork_ev, cs);
   for (int s = 0; s < nside && e == cudaSuccess; ++s) e = cudaStreamWaitEvent(c->side[s], c->fork_ev, 0);
   for (size_t k = 0; k < order.size() && e == cudaSuccess; ++k) {
@@ -926,6 +937,78 @@ int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, dou
 int fockgb_ctx_device(const fock_ctx* c) { return c->device; }
 
 extern "C" {
+
+// Autotuner: coordinate search over the launch parameters of the current
+// precision plan, each candidate re-planned, captured and timed with CUDA
+// events over `reps` builds after one warm-up build.
+int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best) {
+  if (!c || !D_dev || !best) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  reps = std::max(1, reps);
+  const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto measure = [&](float* ms) -> int {
+    int rc = build_plan(c, false);
+    if (rc != FOCK_OK) return rc;
+    rc = fock_build_jk_device(c, D_dev, c->d_G);  // captures + warms up
+    if (rc != FOCK_OK) return rc;
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < reps && rc == FOCK_OK; ++r) rc = fock_build_jk_device(c, D_dev, c->d_G);
+    cudaEventRecord(e1, c->stream);
+    CK(cudaEventSynchronize(e1));
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= reps;
+    return rc;
+  };
+  fock_tuning cur{c->opt.prims_per_slice, c->opt.prims_per_slice_fp32, c->opt.block_threads, c->opt.persistent, 0.f};
+  auto apply = [&](const fock_tuning& t) {
+    c->opt.prims_per_slice = t.prims_per_slice;
+    c->opt.prims_per_slice_fp32 = t.prims_per_slice_fp32;
+    c->opt.block_threads = t.block_threads;
+    c->opt.persistent = t.persistent;
+  };
+  int rc = measure(&cur.ms);
+  const std::vector<int> pps64 = {1, 2, 4}, pps32 = {1, 2, 4, 8}, blk = {64, 128, 256}, per = {0, 1};
+  for (int dim = 0; dim < 4 && rc == FOCK_OK; ++dim) {
+    const std::vector<int>& cand = dim == 0 ? pps64 : dim == 1 ? pps32 : dim == 2 ? blk : per;
+    if (dim == 1 && !mixed) continue;
+    if (dim == 0 && mixed && c->opt.mixed_threshold > 1e20) continue;
+    for (int v : cand) {
+      fock_tuning t = cur;
+      int* f = dim == 0 ? &t.prims_per_slice : dim == 1 ? &t.prims_per_slice_fp32 : dim == 2 ? &t.block_threads : &t.persistent;
+      if (*f == v) continue;
+      *f = v;
+      apply(t);
+      rc = measure(&t.ms);
+      if (rc != FOCK_OK) break;
+      if (t.ms < cur.ms) cur = t;
+    }
+    apply(cur);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  apply(cur);
+  const int rc2 = build_plan(c, false);
+  if (rc != FOCK_OK) return rc;
+  if (rc2 != FOCK_OK) return rc2;
+  *best = cur;
+  return FOCK_OK;
+}
+
+int fock_set_tuning(fock_ctx* c, const fock_tuning* t) {
+  if (!c || !t || t->prims_per_slice < 1 || t->prims_per_slice_fp32 < 1 || t->block_threads < 32 ||
+      t->block_threads > 256 || (t->block_threads & 31))
+    return FOCK_ERR_INVALID_ARG;
+  c->opt.prims_per_slice = t->prims_per_slice;
+  c->opt.prims_per_slice_fp32 = t->prims_per_slice_fp32;
+  c->opt.block_threads = t->block_threads;
+  c->opt.persistent = t->persistent ? 1 : 0;
+  return build_plan(c, false);
+}
+
+int fock_batch_autotune(fock_batch* b, const double* D_dev, int reps, fock_tuning* best);
 
 int fock_profile_build(fock_ctx* c, const double* D_dev, fock_launch_profile* out, int cap) {
   if (!c || !D_dev || (cap > 0 && !out)) return FOCK_ERR_INVALID_ARG;
@@ -1002,6 +1085,7 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       std::vector<Plan> keep_plans = c->plans;
       int* keep_i = c->d_plan_int;
       long long* keep_l = c->d_plan_ll;
+      const size_t keep_q = c->queue_base;
       c->d_plan_int = nullptr;
       c->d_plan_ll = nullptr;
       rc = build_plan(c, true);
@@ -1019,6 +1103,7 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       dfree(c->d_plan_ll);
       c->d_plan_int = keep_i;
       c->d_plan_ll = keep_l;
+      c->queue_base = keep_q;
       c->plans = keep_plans;
       c->opt = keep;
     }
@@ -1473,6 +1558,10 @@ long long fock_batch_launch_count(const fock_batch* b) { return b ? b->c->launch
 
 int fock_batch_build_jk_device(fock_batch* b, const double* D_dev, double* G_dev) {
   return b ? fock_build_jk_device(b->c, D_dev, G_dev) : FOCK_ERR_INVALID_ARG;
+}
+
+int fock_batch_autotune(fock_batch* b, const double* D_dev, int reps, fock_tuning* best) {
+  return b ? fock_autotune(b->c, D_dev, reps, best) : FOCK_ERR_INVALID_ARG;
 }
 
 // Lockstep RHF over the batch (try_scf per molecule, scf/src/lib.rs:73-258).

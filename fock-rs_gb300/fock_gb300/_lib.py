@@ -39,7 +39,8 @@ class Options(C.Structure):
                 ("group_by_contraction", C.c_int), ("max_iters", C.c_int), ("epsilon", C.c_double),
                 ("conv_mode", C.c_int), ("guess", C.c_int), ("diis_len", C.c_int), ("diis_start", C.c_int),
                 ("energy_mode", C.c_int), ("final_fp64", C.c_int), ("device", C.c_int),
-                ("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int)]
+                ("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int),
+                ("block_threads", C.c_int), ("persistent", C.c_int)]
 
 
 class ScfResult(C.Structure):

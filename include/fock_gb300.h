@@ -92,6 +92,8 @@ typedef struct {
   int device;      /* CUDA device ordinal */
   int prims_per_slice;      /* FP64: bra primitive pairs per warp (more warps per heavy quartet) */
   int prims_per_slice_fp32; /* same for FP32 quartets */
+  int block_threads;        /* threads per block of the class launches (64, 128, 256) */
+  int persistent;           /* 1: persistent class launches fed by per-launch work queues */
 } fock_options;
 
 typedef struct {
@@ -240,6 +242,20 @@ int fock_batch_build_jk_device(fock_batch* batch, const double* D_dev, double* G
 /* RHF of every molecule; charges may be NULL (neutral); results[nmol] in the
  * caller's order (energies, iterations, convergence; buffers not filled). */
 int fock_batch_scf(fock_batch* batch, const int* charges, fock_scf_result* results);
+
+/* Autotuner (no counterpart in the reference): launch parameters of the
+ * Fock build -- primitive pairs per lane for FP64 and FP32 quartets (the
+ * "primitives per thread"), threads per block ("quartets per block") and
+ * persistent work-queue launches -- chosen by a coordinate search, each
+ * candidate timed with CUDA events over `reps` builds of the density D_dev
+ * (device, textbook sign).  The best setting stays in the context. */
+typedef struct {
+  int prims_per_slice, prims_per_slice_fp32, block_threads, persistent;
+  float ms; /* time of one build with this setting */
+} fock_tuning;
+int fock_autotune(fock_ctx* ctx, const double* D_dev, int reps, fock_tuning* best);
+int fock_set_tuning(fock_ctx* ctx, const fock_tuning* t);
+int fock_batch_autotune(fock_batch* batch, const double* D_dev, int reps, fock_tuning* best);
 
 const char* fock_strerror(int code);
 
