@@ -38,6 +38,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "ERI+Fock quartets/s (C6H6 RHF/6-31G Fock build)"
 UNIT = "quartets/s"
+BATCH_LEVEL_SHIFT = 1.0  # Eh; SCF level shift of the batched water-cluster workload
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
             "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
 
@@ -139,6 +140,136 @@ def cpu_reference(steps, warmup, sample_w=3, threads=0):
                    "eri_quartets_per_s": rate, "est_full_build_s": t_eri + t_fock}
 
 
+def _event_times(torch, stream, fn, k, w, flush):
+    """Device times (ms) of k calls of fn on ``stream`` after w warm-up calls, L2 flushed before each."""
+    with torch.cuda.stream(stream):
+        for _ in range(w):
+            fn()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
+        for e0, e1 in ev:
+            flush.fill_(1.0)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+    stream.synchronize()
+    return [e0.elapsed_time(e1) for e0, e1 in ev]
+
+
+def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
+    """512 water clusters (H2O)_n, n ~ U{1..8} (seed 0), RHF/6-31G, one batch context.
+
+    Mixed-precision batched SCF (final iterations FP64) gives the converged
+    densities; FP64 and mixed batched Fock builds are timed at those densities;
+    the mixed build's energy error per molecule is 1/2 sum D (G_mixed - G_fp64);
+    ``spot`` molecules are re-solved alone in FP64 and compared with the batch."""
+    from fock_gb300 import basis as B, molecules as M
+    batch = M.water_cluster_batch(512, seed=0)
+    mols = [B.build_atoms("6-31G", Zs, xyz) for Zs, xyz in batch]
+    kw = dict(guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, epsilon=1e-8, max_iters=100,
+              level_shift=BATCH_LEVEL_SHIFT, sign_convention=L.FOCK_SIGN_STANDARD, device=local)
+    out = {"workload": "512 water clusters (H2O)_n, n~U{1..8} seed 0, RHF/6-31G, one batched context"}
+    t0 = time.perf_counter()
+    b = F.FockBatch(mols, **kw)
+    out["create_s"] = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    b.set_stream(stream.cuda_stream)
+    b.set_precision(L.FOCK_PREC_MIXED, F.options().mixed_threshold)
+    t0 = time.perf_counter()
+    rc, res, dens = b.scf(densities=True)
+    torch.cuda.synchronize()
+    out["scf_mixed"] = {"rc": rc, "wall_s": time.perf_counter() - t0, "fock_s": res[0].fock_seconds,
+                        "fock_builds": res[0].fock_builds, "converged": sum(r.converged for r in res),
+                        "iterations_max": max(r.iterations for r in res),
+                        "level_shift_eh": BATCH_LEVEL_SHIFT}
+    D = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+    for off, n, Dm in zip(b.offsets, b.nbf, dens):
+        D[off:off + n * n] = torch.from_numpy(Dm.reshape(-1))
+    G = torch.zeros_like(D)
+    st = b.stats()
+    nq = st["function_quartets_unique"]
+    out["unique_quartets"] = nq
+    res_prec = {}
+    Gs = {}
+    for name, prec in (("fp64", L.FOCK_PREC_FP64), ("mixed", L.FOCK_PREC_MIXED)):
+        b.set_precision(prec, F.options().mixed_threshold)
+        l0 = b.launch_count()
+        t = _event_times(torch, stream, lambda: b.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
+        ms = sum(t) / len(t)
+        res_prec[name] = {"ms_per_build": ms, "quartets_per_s": nq / (ms * 1e-3),
+                          "launches_per_build": (b.launch_count() - l0) // (steps + warmup)}
+        Gs[name] = G.clone()
+    res_prec["mixed"]["speedup_vs_fp64"] = res_prec["fp64"]["ms_per_build"] / res_prec["mixed"]["ms_per_build"]
+    dG = Gs["mixed"] - Gs["fp64"]
+    de = [0.5 * float((D[o:o + n * n] * dG[o:o + n * n]).sum().item()) for o, n in zip(b.offsets, b.nbf)]
+    res_prec["mixed"]["max_single_build_energy_error_eh"] = max(abs(x) for x in de)
+    out.update(res_prec)
+    # spot check: molecules solved alone in FP64 against the batched mixed SCF
+    idx = np.linspace(0, len(mols) - 1, spot).astype(int)
+    worst = 0.0
+    for i in idx:
+        r = F.try_scf(mols[i], 100, 1e-8, 0, **{k: v for k, v in kw.items() if k not in ("max_iters", "epsilon")})
+        if r is not None and r.converged and res[i].converged:
+            worst = max(worst, abs(r.total_energy - res[i].total_energy))
+    out["scf_mixed"]["max_abs_energy_error_vs_single_fp64_eh"] = worst
+    out["scf_mixed"]["spot_checked_molecules"] = [int(i) for i in idx]
+    b.close()
+    return out
+
+
+def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
+    """(H2O)_32 cluster (seed 0), RHF/6-31G* with Cartesian d on O: 608 functions.
+    FP64 and mixed Fock builds at a density of 160 random orthonormal-ish orbitals."""
+    from fock_gb300 import basis as B, molecules as M
+    Zs, xyz = M.water_cluster(32, seed=0)
+    atoms = B.build_atoms("6-31G*", Zs, xyz)
+    ctx = F.FockContext(atoms, sign_convention=L.FOCK_SIGN_STANDARD, device=local)
+    n = ctx.n
+    rng = np.random.default_rng(0)
+    Cm = rng.normal(size=(n, 160)) / np.sqrt(n)
+    D = torch.tensor(2.0 * Cm @ Cm.T, device="cuda")
+    G = torch.empty_like(D)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    st = ctx.stats()
+    nq = st["function_quartets_unique"]
+    out = {"workload": "(H2O)32 seed 0, RHF/6-31G*, %d functions" % n, "unique_quartets": nq}
+    Gs = {}
+    for name, prec in (("fp64", L.FOCK_PREC_FP64), ("mixed", L.FOCK_PREC_MIXED)):
+        ctx.set_precision(prec, F.options().mixed_threshold)
+        t = _event_times(torch, stream, lambda: ctx.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
+        ms = sum(t) / len(t)
+        out[name] = {"ms_per_build": ms, "quartets_per_s": nq / (ms * 1e-3)}
+        Gs[name] = G.clone()
+    out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_build"] / out["mixed"]["ms_per_build"]
+    out["mixed"]["single_build_energy_error_eh"] = abs(0.5 * float((D * (Gs["mixed"] - Gs["fp64"])).sum().item()))
+    ctx.close()
+    return out
+
+
+def octane_gradient_workload(torch, F, L, local):
+    """n-octane C8H18 (seed 0, sigma 0.05 A), RHF/6-31G: FP64 SCF, then the
+    nuclear gradient through fock_energy_backward (derivative ERIs contracted
+    with the density on the fly + one-electron derivatives), wall-timed."""
+    from fock_gb300 import basis as B, molecules as M
+    Zs, xyz = M.octane(seed=0)
+    atoms = B.build_atoms("6-31G", Zs, xyz)
+    with F.FockContext(atoms, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1,
+                       max_iters=100, epsilon=1e-10, device=local) as ctx:
+        t0 = time.perf_counter()
+        rc, r, eps, Dm, Cm = ctx.scf(0)
+        scf_s = time.perf_counter() - t0
+        ctx.energy_backward()  # warm-up (plans the derivative launches)
+        torch.cuda.synchronize()
+        reps = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            g = ctx.energy_backward()
+            reps.append(time.perf_counter() - t0)
+    return {"workload": "n-octane C8H18 seed 0, RHF/6-31G, 108 functions", "scf_s": scf_s, "scf_rc": rc,
+            "energy": r.total_energy, "iterations": r.iterations, "gradient_s": min(reps),
+            "max_abs_gradient": float(np.abs(g).max()), "net_force": float(np.abs(g.sum(axis=0)).max())}
+
+
 def run_reference_arm(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -162,6 +293,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scf", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the batch, (H2O)32 and gradient workloads")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -327,6 +459,16 @@ def main():
             cpu = cb
         except Exception as ex:  # baseline is reported, never fatal
             cpu = {"value": None, "error": str(ex)[:200]}
+
+    if rank == 0 and not args.no_extra:
+        extra["workloads"] = {}
+        for key, fn in (("batch_512_water_clusters_631g", lambda: batch_workload(torch, F, L, local, flush)),
+                        ("water32_631gs", lambda: water32_workload(torch, F, L, local, flush)),
+                        ("octane_631g_gradient", lambda: octane_gradient_workload(torch, F, L, local))):
+            try:
+                extra["workloads"][key] = fn()
+            except Exception as ex:  # reported beside the headline, never fatal
+                extra["workloads"][key] = {"error": repr(ex)[:300]}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -183,6 +183,9 @@ struct fock_ctx {
   // molecules (one for fock_ctx_create, many for a batch)
   int nmol = 1;
   std::vector<int> mol_shell0, mol_nbf, mol_f0;
+  // per-molecule plan state set by the batched SCF (empty: every molecule at
+  // opt.precision): 0 = left out, 1 = mixed split, 2 = FP64 only
+  std::vector<unsigned char> mol_mode;
   std::vector<long long> mol_off;  // nmol + 1 block offsets
   long long total_elems = 0;
   long long* d_mol_off = nullptr;
@@ -271,10 +274,20 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   dfree(c->d_plan_ll);
   c->plans.clear();
   const double tau = for_tensor ? 0.0 : c->opt.schwarz_eps;
-  const bool mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
+  const bool ctx_mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
+  // plan state of molecule m (see fock_ctx::mol_mode)
+  auto mode_of = [&](int m) -> int {
+    if (for_tensor || c->mol_mode.empty()) return ctx_mixed ? 1 : 2;
+    return c->mol_mode[m];
+  };
+  bool mixed = false;
+  for (int m = 0; m < c->nmol; ++m) mixed |= mode_of(m) == 1;
   const double tmix = c->opt.mixed_threshold;
   const int npairs = (int)c->hpairs.size();
   const int nmol = c->nmol;
+  long long row_counter = 0;  // global row count (shard assignment)
+  if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
+    return FOCK_ERR_INVALID_ARG;
   // pairs per (molecule, class), sorted by Q descending (ties by index)
   std::vector<std::vector<std::vector<int>>> cls(nmol, std::vector<std::vector<int>>(kNumPairClasses));
   for (int p = 0; p < npairs; ++p)
@@ -331,6 +344,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           for (int m = 0; m < nmol; ++m) {
             const std::vector<int>& bras = cls[m][X];
             if (bras.empty() || cls[m][Y].empty()) continue;
+            const int md = mode_of(m);
+            if (md == 0 || (prec == 1 && md == 2)) continue;
             std::vector<int> g;  // this molecule's kets of the group, Q order
             for (int p : cls[m][Y])
               if (key < 0 || c->hpairs[p].nprim == key) g.push_back(p);
@@ -364,11 +379,14 @@ int build_plan(fock_ctx* c, bool for_tensor) {
               };
               size_t n_all = std::min(n_order, cnt_ge(tau));
               size_t beg = 0, end = n_all;
-              if (mixed) {
+              if (md == 1) {
                 size_t n64 = std::min(n_all, cnt_ge(tmix));
                 if (prec == 0) end = n64; else beg = n64;
               }
               if (end <= beg) continue;
+              // multi-rank build: every shard keeps the rows of its residue class
+              if (!for_tensor && c->opt.shard_count > 1 && (row_counter++ % c->opt.shard_count) != c->opt.shard_index)
+                continue;
               used = true;
               rbra.push_back(bi);
               rbeg.push_back(base + (int)beg);
@@ -535,6 +553,9 @@ void fock_options_default(fock_options* o) {
   o->prims_per_slice_fp32 = 4;
   o->block_threads = 128;
   o->persistent = 0;
+  o->shard_index = 0;
+  o->shard_count = 1;
+  o->level_shift = 0.0;
   o->device = 0;
 }
 
@@ -627,6 +648,7 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   for (int a = 0; a < natom; ++a)
     if (!std::isfinite(atoms[a].x) || !std::isfinite(atoms[a].y) || !std::isfinite(atoms[a].z) || atoms[a].Z < 0)
       return FOCK_ERR_INVALID_ARG;
+  if (o.shard_count < 1 || o.shard_index < 0 || o.shard_index >= o.shard_count) return FOCK_ERR_INVALID_ARG;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return FOCK_ERR_NO_DEVICE;
   if (o.device < 0 || o.device >= ndev) return FOCK_ERR_INVALID_ARG;
@@ -842,6 +864,7 @@ int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
   CK(cudaSetDevice(c->device));
   c->opt.precision = precision;
   c->opt.mixed_threshold = mixed_threshold;
+  c->mol_mode.clear();
   return build_plan(c, false);
 }
 
@@ -1153,7 +1176,7 @@ int fock_one_electron(fock_ctx* c, double* S, double* T, double* V) {
 }
 
 int fock_gradient(fock_ctx* c, const double* D, const double* W, double* grad) {
-  if (!c || !D || !W || !grad) return FOCK_ERR_INVALID_ARG;
+  if (!c || !D || !W || !grad || c->opt.shard_count > 1 || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
   if (c->opt.eri_mode != FOCK_ERI_EXACT) return FOCK_ERR_INVALID_ARG;
   for (const HostShell& h : c->shells)
@@ -1247,7 +1270,7 @@ int fock_measure_fma_peak(int device, int fp64, double* gflops) {
 // RHF (scf/src/lib.rs:73-258) on the device.  Column-major n x n buffers.
 // ---------------------------------------------------------------------------
 int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
-  if (!c || !res) return FOCK_ERR_INVALID_ARG;
+  if (!c || !res || c->opt.shard_count > 1 || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
   auto t_start = std::chrono::steady_clock::now();
   const int n = c->nbf;
@@ -1280,6 +1303,8 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   double *F = mk(nn), *Fd = mk(nn), *G = mk(nn), *Dm = mk(nn), *Dn = mk(nn), *C = mk(nn), *T1 = mk(nn), *T2 = mk(nn);
   double *Fring = mk(nn * ring), *Ering = mk(nn * ring), *Bm = mk((size_t)ring * ring), *coef = mk(ring + 1);
   double* scal = mk(4);  // [0] E_cur, [1] E_ref, [2] max|e| bits
+  const double shift = c->opt.level_shift;
+  double* Fsh = shift != 0.0 ? mk(nn) : F;
   int* d_order = nullptr;
   int* d_info = nullptr;
   cudaError_t e = dalloc(&d_order, ring);
@@ -1391,6 +1416,13 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       c->launches += 2;
       Fuse = Fd;
     }
+    if (shift != 0.0) {  // F + b (S - 1/2 S D S)
+      gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, S, Dm, T1);
+      gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, S, T2);
+      cku(k_level_shift(Fuse, S, T2, shift, (long long)nn, Fsh, s));
+      c->launches++;
+      Fuse = Fsh;
+    }
     density_from(Fuse, Dn);
     cku(k_energy(Dn, H, G, (int)nn, scal + 1, s));        // reference energy: new D, old G
     c->launches++;
@@ -1446,7 +1478,8 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
         for (int i = 0; i < n; ++i)
           for (int k = 0; k < n; ++k)
             res->coefficient_matrix[(size_t)i * n + k] = hC[(size_t)k * n + i] * (flip ? c->fsign[i] : 1.0);
-      if (res->orbital_energies) std::memcpy(res->orbital_energies, evals.data(), n * 8);
+      if (res->orbital_energies)  // the level shift lifted the virtual orbitals by b
+        for (int k = 0; k < n; ++k) res->orbital_energies[k] = evals[k] - (k >= nocc ? shift : 0.0);
       result = FOCK_OK;
       break;
     }
@@ -1621,6 +1654,8 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   double *F = (double*)mk(TB), *Fd = (double*)mk(TB), *G = (double*)mk(TB), *Dm = (double*)mk(TB);
   double *Dn = (double*)mk(TB), *Cm = (double*)mk(TB), *T1 = (double*)mk(TB), *T2 = (double*)mk(TB);
   double *Fring = (double*)mk(TB * ring), *Ering = (double*)mk(TB * ring);
+  const double shift = c->opt.level_shift;
+  double* Fsh = shift != 0.0 ? (double*)mk(TB) : F;
   double* Bm = (double*)mk((size_t)nmol * ring * ring * 8);
   double* coef = (double*)mk((size_t)nmol * (ring + 1) * 8);
   double* ecur = (double*)mk((size_t)nmol * 8);
@@ -1702,10 +1737,16 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   c->launches++;
   density_from(F, Dm);
 
+  // Per-molecule plan state: 1 = mixed precision, 2 = FP64, 0 = out of the
+  // plan (converged, result frozen).  A mixed molecule becomes "ready" once its
+  // DIIS error is below kMixedSwitch; ready and finished molecules change state
+  // together at the next re-plan, which happens once they are a quarter of the
+  // molecules in the plan (or every mixed molecule is ready), so that plans are
+  // rebuilt O(log nmol) times while the stragglers stop paying for the rest.
   const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
-  const double mixed_th = c->opt.mixed_threshold;
-  bool fp64_phase = !mixed;
-  std::vector<int> done(nmol, 0);
+  const bool refine = mixed && c->opt.final_fp64;
+  std::vector<unsigned char> mode(nmol, mixed ? 1 : 2);
+  std::vector<int> done(nmol, 0), ready(nmol, 0);
   std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol);
   std::vector<unsigned long long> hb(nmol);
   for (int k = 0; k < nmol; ++k) {
@@ -1716,14 +1757,35 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     o.nuclear_repulsion = vnn[k];
   }
   std::vector<int> order;
-  int next_slot = 0, builds = 0, ndone = 0, it_last = 0;
+  int next_slot = 0, builds = 0, ndone = 0, replans = 0;
   double fock_ms = 0.0;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
   cudaEventCreate(&ev1);
   int result = FOCK_OK;
+  auto finish = [&](int k, int iter, bool conv) {
+    fock_scf_result& o = results[b->perm[k]];
+    const double e = c->opt.energy_mode == 0 ? hr[k] : he[k];
+    o.electronic_energy = e;
+    o.total_energy = e + vnn[k];
+    o.iterations = iter;
+    o.converged = conv ? 1 : 0;
+    if (o.density_matrix) {  // this molecule's block of the density of the reported energy
+      const int nk = c->mol_nbf[k];
+      std::vector<double> hD((size_t)nk * nk);
+      cku(cudaMemcpyAsync(hD.data(), (c->opt.energy_mode == 0 ? Dn : Dm) + c->mol_off[k], hD.size() * 8,
+                          cudaMemcpyDeviceToHost, s));
+      cku(cudaStreamSynchronize(s));
+      const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
+      const double* sg = c->fsign.data() + c->mol_f0[k];
+      for (int i = 0; i < nk; ++i)
+        for (int j = 0; j < nk; ++j)
+          o.density_matrix[(size_t)i * nk + j] = hD[(size_t)j * nk + i] * (flip ? sg[i] * sg[j] : 1.0);
+    }
+    done[k] = 1;
+    ++ndone;
+  };
   for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
-    it_last = iter;
     cudaEventRecord(ev0, s);
     { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
@@ -1749,6 +1811,13 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       c->launches += 2;
       Fuse = Fd;
     }
+    if (shift != 0.0) {  // F + b (S - 1/2 S D S), every block
+      for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, S, Dm, T1);
+      for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
+      cku(k_level_shift(Fuse, S, T2, shift, T, Fsh, s));
+      c->launches++;
+      Fuse = Fsh;
+    }
     density_from(Fuse, Dn);
     cku(kb_energy(Dn, H, G, c->d_mol_off, nmol, eref, s));
     c->launches++;
@@ -1760,47 +1829,50 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev0, ev1);
     fock_ms += ms;
-    double maxerr = 0.0;
     bool diverged = false;
     for (int k = 0; k < nmol; ++k) {
       std::memcpy(&errv[k], &hb[k], 8);
-      if (!done[k]) maxerr = std::max(maxerr, errv[k]);
       if (!done[k] && !std::isfinite(errv[k])) diverged = true;
     }
     if (diverged) { result = FOCK_ERR_DIVERGED; break; }
-    if (!fp64_phase && (maxerr < kMixedSwitch || iter >= c->opt.max_iters / 2)) {
-      // all molecules close to convergence: finish in FP64
-      int r = fock_set_precision(c, FOCK_PREC_FP64, mixed_th);
-      if (r != FOCK_OK) { fail = r; break; }
-      fp64_phase = true;
-      for (int k = 0; k < nmol; ++k) eprev[k] = he[k];
-      std::swap(Dm, Dn);
-      continue;
-    }
-    if (fp64_phase) {
-      for (int k = 0; k < nmol; ++k) {
-        if (done[k]) continue;
+    const bool last = iter == c->opt.max_iters;
+    int n_in = 0, n_mixed = 0, n_ready = 0, n_stale = 0;
+    for (int k = 0; k < nmol; ++k) {
+      if (mode[k] == 0) continue;
+      ++n_in;
+      if (!done[k]) {
         bool conv;
         if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) conv = errv[k] < c->opt.epsilon;
         else conv = iter > 0 && std::fabs(he[k] - eprev[k]) < c->opt.epsilon && errv[k] < std::sqrt(c->opt.epsilon);
-        if (conv || iter == c->opt.max_iters) {
-          fock_scf_result& o = results[b->perm[k]];
-          const double e = c->opt.energy_mode == 0 ? hr[k] : he[k];
-          o.electronic_energy = e;
-          o.total_energy = e + vnn[k];
-          o.iterations = iter;
-          o.converged = conv ? 1 : 0;
-          done[k] = 1;
-          ++ndone;
+        if (mode[k] == 1 && refine && !last) {
+          // mixed phase: close to convergence (or half the iterations gone) -> FP64 at the next re-plan
+          if (conv || errv[k] < kMixedSwitch || iter >= c->opt.max_iters / 2) ready[k] = 1;
+        } else if (conv || last) {
+          finish(k, iter, conv);
         }
       }
-      if (ndone == nmol) break;
+      if (mode[k] == 1 && !done[k]) { ++n_mixed; n_ready += ready[k]; }
+      if (done[k]) ++n_stale;
+    }
+    if (ndone == nmol) break;
+    if ((n_mixed > 0 && n_ready == n_mixed) || n_ready + n_stale >= std::max(1, n_in / 4)) {
+      for (int k = 0; k < nmol; ++k) {
+        if (done[k]) mode[k] = 0;
+        else if (ready[k]) { mode[k] = 2; ready[k] = 0; }
+      }
+      c->mol_mode = mode;
+      int r = build_plan(c, false);
+      if (r != FOCK_OK) { fail = r; break; }
+      ++replans;
     }
     for (int k = 0; k < nmol; ++k) eprev[k] = he[k];
     std::swap(Dm, Dn);
   }
-  (void)it_last;
-  if (mixed && fp64_phase) fock_set_precision(c, FOCK_PREC_MIXED, mixed_th);
+  if (replans) {  // back to the context's own plan
+    c->mol_mode.clear();
+    int r = build_plan(c, false);
+    if (r != FOCK_OK && fail == FOCK_OK) fail = r;
+  }
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
   if (sp) cusolverDnDestroyParams(sp);

@@ -15,6 +15,13 @@ __global__ void add_kernel(const double* a, const double* b, double* c, int nn) 
   if (t < nn) c[t] = a[t] + b[t];
 }
 
+// Level-shifted Fock matrix F + b S - (b/2) S D S.
+__global__ void level_shift_kernel(const double* F, const double* S, const double* SDS, double b, long long nn,
+                                   double* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nn) out[t] = F[t] + b * S[t] - 0.5 * b * SDS[t];
+}
+
 // G = M + M^T (row-major M); optional output sign s_i s_j.
 __global__ void symmetrize_kernel(const double* M, double* G, int n) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -189,6 +196,11 @@ static unsigned blocks_for(long long n, int thr) { return (unsigned)((n + thr - 
 
 cudaError_t k_add(const double* a, const double* b, double* c, int nn, cudaStream_t s) {
   add_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, c, nn);
+  return cudaGetLastError();
+}
+cudaError_t k_level_shift(const double* F, const double* S, const double* SDS, double b, long long nn, double* out,
+                          cudaStream_t s) {
+  level_shift_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(F, S, SDS, b, nn, out);
   return cudaGetLastError();
 }
 cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s) {

@@ -213,12 +213,19 @@ class FockBatch:
         check(lib().fock_batch_build_jk_device(self.handle, C.c_void_p(d_ptr), C.c_void_p(g_ptr)),
               "fock_batch_build_jk_device")
 
-    def scf(self, charges=None):
+    def scf(self, charges=None, densities=False):
+        """(rc, results); with ``densities`` also the list of final density matrices."""
         n = len(self.molecules)
         res = (_lib.ScfResult * n)()
+        dens = []
+        if densities:
+            for i in range(n):
+                dens.append(np.zeros((self.nbf[i], self.nbf[i])))
+                res[i].density_matrix = _dp(dens[i])
         ch = (C.c_int * n)(*(charges or [0] * n)) if charges is not None else None
         rc = lib().fock_batch_scf(self.handle, ch, res)
-        return rc, [res[i] for i in range(n)]
+        out = [res[i] for i in range(n)]
+        return (rc, out, dens) if densities else (rc, out)
 
 
 class ElectronTensor:

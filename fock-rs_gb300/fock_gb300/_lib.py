@@ -40,7 +40,8 @@ class Options(C.Structure):
                 ("conv_mode", C.c_int), ("guess", C.c_int), ("diis_len", C.c_int), ("diis_start", C.c_int),
                 ("energy_mode", C.c_int), ("final_fp64", C.c_int), ("device", C.c_int),
                 ("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int),
-                ("block_threads", C.c_int), ("persistent", C.c_int)]
+                ("block_threads", C.c_int), ("persistent", C.c_int),
+                ("shard_index", C.c_int), ("shard_count", C.c_int), ("level_shift", C.c_double)]
 
 
 class ScfResult(C.Structure):

@@ -94,6 +94,13 @@ typedef struct {
   int prims_per_slice_fp32; /* same for FP32 quartets */
   int block_threads;        /* threads per block of the class launches (64, 128, 256) */
   int persistent;           /* 1: persistent class launches fed by per-launch work queues */
+  int shard_index;          /* multi-rank Fock build: this context computes the rows r of every */
+  int shard_count;          /* launch with r % shard_count == shard_index (G is then a partial sum;
+                               summing the partial G of all shards, e.g. by an all-reduce, gives G) */
+  double level_shift;       /* SCF level shift b (Eh): the matrix diagonalised each iteration is
+                               F + b (S - 1/2 S D S), which lifts the virtual orbitals by b and damps
+                               occupied-virtual mixing.  Self-consistent solutions are unchanged;
+                               reported orbital energies are unshifted.  0 = the reference's loop. */
 } fock_options;
 
 typedef struct {
@@ -240,7 +247,9 @@ long long fock_batch_launch_count(const fock_batch* batch);
 /* G = J - K/2 for every molecule, packed blocks (textbook sign convention). */
 int fock_batch_build_jk_device(fock_batch* batch, const double* D_dev, double* G_dev);
 /* RHF of every molecule; charges may be NULL (neutral); results[nmol] in the
- * caller's order (energies, iterations, convergence; buffers not filled). */
+ * caller's order (energies, iterations, convergence).  A non-NULL
+ * results[m].density_matrix (n_m x n_m doubles) receives molecule m's final
+ * density; orbital_energies and coefficient_matrix are not filled. */
 int fock_batch_scf(fock_batch* batch, const int* charges, fock_scf_result* results);
 
 /* Autotuner (no counterpart in the reference): launch parameters of the

@@ -527,7 +527,8 @@ void g_from_tensor(const double* eri, const double* D, size_t n, double* G) {
 
 // Integral-direct G = J - 1/2 K over the unique function quartets
 // (i>=j, k>=l, ij>=kl), each digested into all eight images.
-void g_direct(const std::vector<Func>& fs, const double* D, int flags, double schwarz, double* G) {
+void g_direct(const std::vector<Func>& fs, const double* D, int flags, double schwarz, double* G, int rank = 0,
+              int nranks = 1) {
   size_t n = fs.size();
   std::vector<std::pair<int, int>> pairs;
   for (size_t i = 0; i < n; ++i)
@@ -543,6 +544,7 @@ void g_direct(const std::vector<Func>& fs, const double* D, int flags, double sc
     std::vector<double> Ml(n * n, 0.0);
 #pragma omp for schedule(dynamic, 1)
     for (long long P = np - 1; P >= 0; --P) {
+      if (P % nranks != rank) continue;  // shard of a multi-rank build
       int i = pairs[P].first, j = pairs[P].second;
       for (long long Q = 0; Q <= P; ++Q) {
         int k = pairs[Q].first, l = pairs[Q].second;
@@ -694,6 +696,16 @@ int orc_eri_tensor(const orc_basis* b, int flags, double schwarz, double* out) {
   init_lut();
   std::vector<Func> fs = load_basis(b);
   eri_tensor(fs, flags, schwarz, out);
+  return 0;
+}
+
+// Partial G of shard `rank` of `nranks` (outer pair index P % nranks == rank):
+// the sum over all shards is G.
+int orc_jk_shard(const orc_basis* b, const double* D, int flags, double schwarz, int rank, int nranks, double* G) {
+  if (nranks < 1 || rank < 0 || rank >= nranks) return -1;
+  init_lut();
+  std::vector<Func> fs = load_basis(b);
+  g_direct(fs, D, flags, schwarz, G, rank, nranks);
   return 0;
 }
 

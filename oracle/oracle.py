@@ -80,6 +80,7 @@ def lib():
         L.orc_eri.argtypes = [C.POINTER(_Basis), C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]
         L.orc_eri_tensor.argtypes = [C.POINTER(_Basis), C.c_int, C.c_double, dp]
         L.orc_jk.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_double, dp]
+        L.orc_jk_shard.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_double, C.c_int, C.c_int, dp]
         L.orc_g_from_tensor.argtypes = [dp, dp, C.c_int, dp]
         L.orc_one_electron.argtypes = [C.POINTER(_Basis), C.c_int, dp, dp, C.c_int, dp, dp, dp]
         L.orc_eig.argtypes = [C.c_int, dp, dp, dp]
@@ -133,6 +134,15 @@ def jk(ob, D, flags=EXACT, schwarz=-1.0):
     D = np.ascontiguousarray(D, dtype=np.float64)
     G = np.zeros((ob.n, ob.n))
     lib().orc_jk(C.byref(ob.s), _dp(D), flags, schwarz, _dp(G))
+    return G
+
+
+def jk_shard(ob, D, rank, nranks, flags=EXACT, schwarz=-1.0):
+    """Partial G of one shard (bra pair index P % nranks == rank); shards sum to jk()."""
+    D = np.ascontiguousarray(D, dtype=np.float64)
+    G = np.zeros((ob.n, ob.n))
+    if lib().orc_jk_shard(C.byref(ob.s), _dp(D), flags, schwarz, rank, nranks, _dp(G)) != 0:
+        raise ValueError("invalid shard %d of %d" % (rank, nranks))
     return G
 
 

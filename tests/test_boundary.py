@@ -32,6 +32,7 @@ def test_options_defaults_match_reference_constants(gpu_lib):
     assert (o.diis_len, o.diis_start) == (16, 5)          # scf/src/lib.rs:197,202
     assert o.guess == 0 and o.conv_mode == 0               # GWH, commutator
     assert o.sign_convention == 0 and o.precision == 0
+    assert (o.shard_index, o.shard_count) == (0, 1)       # one rank builds all rows
 
 
 def test_invalid_input_returns_codes_not_abort(gpu_lib):
@@ -49,6 +50,11 @@ def test_invalid_input_returns_codes_not_abort(gpu_lib):
     sh = (L.Shell * 1)(L.Shell(0, 1, 0, dp(bad), dp(c)))
     assert gpu_lib.fock_ctx_create(atoms, 1, sh, 1, None, C.byref(h)) == -1  # non-positive exponent
     assert gpu_lib.fock_ctx_create(atoms, 0, sh, 1, None, C.byref(h)) == -1
+    sh = (L.Shell * 1)(L.Shell(0, 1, 0, dp(e), dp(c)))
+    from fock_gb300 import options
+    for idx, cnt in [(2, 2), (-1, 2), (0, 0)]:  # shard outside [0, count)
+        o = options(shard_index=idx, shard_count=cnt)
+        assert gpu_lib.fock_ctx_create(atoms, 1, sh, 1, C.byref(o), C.byref(h)) == -1
     assert gpu_lib.fock_strerror(-5) == b"SCF diverged (DIIS error not a normal number)"
 
 
