@@ -16,6 +16,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdlib>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -148,6 +149,32 @@ void dfree(T*& p) {
 
 }  // namespace
 
+// Screened rows of the quartet plans (see build_catalog).
+struct CatSeg {
+  int mol;         // molecule of the segment
+  long long ket0;  // first ket of the segment in PlanCatalog::kets
+  int nket;        // kets of the molecule in the group (Q order)
+  long long row0;  // first row in PlanCatalog::rbra / rall / r64
+  int nrow;
+};
+struct CatGroup {  // one launch group: bra class, ket class, ket primitive-pair count
+  int la, lb, lc, ld;
+  std::vector<CatSeg> segs;
+};
+struct PlanCatalog {
+  bool valid = false;
+  double tau = -1.0, tmix = -1.0;
+  bool grouping = true;
+  std::vector<CatGroup> groups;
+  std::vector<int> kets;        // ket pair ids, segment after segment
+  std::vector<long long> kpre;  // kpre[i] = primitive pairs of kets[0..i)
+  std::vector<int> rbra;        // per row: bra pair
+  std::vector<int> rall;        // kets that pass canonical order + Schwarz (a prefix of the segment)
+  std::vector<int> r64;         // of those, kets above the mixed threshold (FP64 in mixed mode)
+  long long total_shell_quartets = 0;
+  long long function_quartets_unique = 0;
+};
+
 struct fock_ctx {
   fock_options opt;
   int device = 0;
@@ -186,6 +213,7 @@ struct fock_ctx {
   // per-molecule plan state set by the batched SCF (empty: every molecule at
   // opt.precision): 0 = left out, 1 = mixed split, 2 = FP64 only
   std::vector<unsigned char> mol_mode;
+  PlanCatalog catalog;
   std::vector<long long> mol_off;  // nmol + 1 block offsets
   long long total_elems = 0;
   long long* d_mol_off = nullptr;
@@ -267,56 +295,44 @@ long long setup_flops(int la, int lb, int lc, int ld) {
 
 int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
 
-// Build the quartet plans from the Schwarz factors.
-int build_plan(fock_ctx* c, bool for_tensor) {
-  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
-  dfree(c->d_plan_int);
-  dfree(c->d_plan_ll);
-  c->plans.clear();
-  const double tau = for_tensor ? 0.0 : c->opt.schwarz_eps;
-  const bool ctx_mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
-  // plan state of molecule m (see fock_ctx::mol_mode)
-  auto mode_of = [&](int m) -> int {
-    if (for_tensor || c->mol_mode.empty()) return ctx_mixed ? 1 : 2;
-    return c->mol_mode[m];
-  };
-  bool mixed = false;
-  for (int m = 0; m < c->nmol; ++m) mixed |= mode_of(m) == 1;
-  const double tmix = c->opt.mixed_threshold;
+// Every screened shell-pair row of every launch group, independent of the
+// per-molecule modes and the shard: built once per (Schwarz threshold, mixed
+// threshold, grouping) and re-assembled into launch plans by build_plan, so
+// that the batched SCF can drop converged molecules or move molecules to FP64
+// without redoing the per-row searches.
+static void build_catalog(const fock_ctx* c, double tau, double tmix, bool grouping, PlanCatalog& cat) {
+  cat = PlanCatalog();
+  cat.tau = tau;
+  cat.tmix = tmix;
+  cat.grouping = grouping;
   const int npairs = (int)c->hpairs.size();
   const int nmol = c->nmol;
-  long long row_counter = 0;  // global row count (shard assignment)
-  if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
-    return FOCK_ERR_INVALID_ARG;
   // pairs per (molecule, class), sorted by Q descending (ties by index)
   std::vector<std::vector<std::vector<int>>> cls(nmol, std::vector<std::vector<int>>(kNumPairClasses));
-  for (int p = 0; p < npairs; ++p)
-    if (c->hpairs[p].nprim > 0) cls[c->shells[c->hpairs[p].sa].mol][c->hpairs[p].cls].push_back(p);
+  std::vector<std::vector<long long>> ncls(nmol, std::vector<long long>(kNumPairClasses, 0));
+  for (int p = 0; p < npairs; ++p) {
+    const int m = c->shells[c->hpairs[p].sa].mol;
+    ncls[m][c->hpairs[p].cls]++;
+    if (c->hpairs[p].nprim > 0) cls[m][c->hpairs[p].cls].push_back(p);
+  }
   std::vector<int> rank(npairs, -1);
   for (auto& mc : cls)
     for (auto& v : mc) {
-      std::stable_sort(v.begin(), v.end(), [&](int a, int b) { return c->Q[a] > c->Q[b]; });
+      std::stable_sort(v.begin(), v.end(), [&](int x, int y) { return c->Q[x] > c->Q[y]; });
       for (size_t r = 0; r < v.size(); ++r) rank[v[r]] = (int)r;
     }
-  std::vector<int> ints;
-  std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
-  std::vector<Pending> pend;
-  fock_stats st{};
-  st.shell_pairs = npairs;
-  st.prim_pairs = c->nprim_pairs;
   // every shell quartet of every molecule (pairs whose primitive pairs were
   // all dropped count as screened)
-  long long total_shell_quartets = 0;
   for (int m = 0; m < nmol; ++m) {
     const long long nf = c->mol_nbf[m], nfp = nf * (nf + 1) / 2;
-    st.function_quartets_unique += nfp * (nfp + 1) / 2;
-    std::vector<long long> ncls(kNumPairClasses, 0);
-    for (const PairInfo& p : c->hpairs)
-      if (c->shells[p.sa].mol == m) ncls[p.cls]++;
+    cat.function_quartets_unique += nfp * (nfp + 1) / 2;
     for (int X = 0; X < kNumPairClasses; ++X)
-      for (int Y = 0; Y <= X; ++Y) total_shell_quartets += (X == Y) ? ncls[X] * (ncls[X] + 1) / 2 : ncls[X] * ncls[Y];
+      for (int Y = 0; Y <= X; ++Y)
+        cat.total_shell_quartets += (X == Y) ? ncls[m][X] * (ncls[m][X] + 1) / 2 : ncls[m][X] * ncls[m][Y];
   }
+  cat.kpre.push_back(0);
+  std::vector<float> gq;
+  std::vector<int> grank, g;
   for (int X = 0; X < kNumPairClasses; ++X) {
     for (int Y = 0; Y <= X; ++Y) {
       int la = 0, lb = 0, lc = 0, ld = 0;
@@ -327,7 +343,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
         }
       // ket groups by primitive-pair count (uniform inner loops); -1 = all
       std::vector<int> keys;
-      if (c->opt.group_by_contraction) {
+      if (grouping) {
         for (int m = 0; m < nmol; ++m)
           for (int p : cls[m][Y]) keys.push_back(c->hpairs[p].nprim);
         std::sort(keys.begin(), keys.end());
@@ -335,107 +351,169 @@ int build_plan(fock_ctx* c, bool for_tensor) {
       } else {
         keys.push_back(-1);
       }
-      int hrr = 0, neri = 0;
-      const int vrr = class_vrr_flops(la, lb, lc, ld, &hrr, &neri);
       for (int key : keys) {
-        for (int prec = 0; prec < (mixed ? 2 : 1); ++prec) {
-          std::vector<int> rbra, rbeg, rcnt, kets;
-          long long q = 0, pq = 0;
-          for (int m = 0; m < nmol; ++m) {
-            const std::vector<int>& bras = cls[m][X];
-            if (bras.empty() || cls[m][Y].empty()) continue;
-            const int md = mode_of(m);
-            if (md == 0 || (prec == 1 && md == 2)) continue;
-            std::vector<int> g;  // this molecule's kets of the group, Q order
-            for (int p : cls[m][Y])
-              if (key < 0 || c->hpairs[p].nprim == key) g.push_back(p);
-            if (g.empty()) continue;
-            std::vector<float> gq(g.size());
-            std::vector<int> grank(g.size());
-            std::vector<long long> gprim(g.size() + 1, 0);
-            for (size_t k = 0; k < g.size(); ++k) {
-              gq[k] = c->Q[g[k]];
-              grank[k] = rank[g[k]];
-              gprim[k + 1] = gprim[k] + c->hpairs[g[k]].nprim;
-            }
-            const int base = (int)kets.size();
-            bool used = false;
-            for (int bi : bras) {
-              const double Qb = c->Q[bi];
-              // kets allowed by the canonical order (same class: rank <= rank(bra))
-              size_t n_order = g.size();
-              if (X == Y) n_order = std::upper_bound(grank.begin(), grank.end(), rank[bi]) - grank.begin();
-              // Schwarz: Q_b Q_k >= threshold  (gq descending)
-              auto cnt_ge = [&](double thr) -> size_t {
-                if (thr <= 0.0) return g.size();
-                if (Qb <= 0.0) return 0;
-                const double need = thr / Qb;
-                size_t lo = 0, hi = g.size();
-                while (lo < hi) {
-                  size_t mid = (lo + hi) / 2;
-                  if ((double)gq[mid] >= need) lo = mid + 1; else hi = mid;
-                }
-                return lo;
-              };
-              size_t n_all = std::min(n_order, cnt_ge(tau));
-              size_t beg = 0, end = n_all;
-              if (md == 1) {
-                size_t n64 = std::min(n_all, cnt_ge(tmix));
-                if (prec == 0) end = n64; else beg = n64;
+        CatGroup G;
+        G.la = la; G.lb = lb; G.lc = lc; G.ld = ld;
+        for (int m = 0; m < nmol; ++m) {
+          const std::vector<int>& bras = cls[m][X];
+          if (bras.empty() || cls[m][Y].empty()) continue;
+          g.clear();  // this molecule's kets of the group, Q order
+          for (int p : cls[m][Y])
+            if (key < 0 || c->hpairs[p].nprim == key) g.push_back(p);
+          if (g.empty()) continue;
+          gq.resize(g.size());
+          grank.resize(g.size());
+          for (size_t k = 0; k < g.size(); ++k) { gq[k] = c->Q[g[k]]; grank[k] = rank[g[k]]; }
+          CatSeg sg;
+          sg.mol = m;
+          sg.ket0 = (long long)cat.kets.size();
+          sg.nket = (int)g.size();
+          sg.row0 = (long long)cat.rbra.size();
+          for (int bi : bras) {
+            const double Qb = c->Q[bi];
+            // kets allowed by the canonical order (same class: rank <= rank(bra))
+            size_t n_order = g.size();
+            if (X == Y) n_order = std::upper_bound(grank.begin(), grank.end(), rank[bi]) - grank.begin();
+            // Schwarz: Q_b Q_k >= threshold  (gq descending)
+            auto cnt_ge = [&](double thr) -> size_t {
+              if (thr <= 0.0) return g.size();
+              if (Qb <= 0.0) return 0;
+              const double need = thr / Qb;
+              size_t lo = 0, hi = g.size();
+              while (lo < hi) {
+                size_t mid = (lo + hi) / 2;
+                if ((double)gq[mid] >= need) lo = mid + 1; else hi = mid;
               }
-              if (end <= beg) continue;
-              // multi-rank build: every shard keeps the rows of its residue class
-              if (!for_tensor && c->opt.shard_count > 1 && (row_counter++ % c->opt.shard_count) != c->opt.shard_index)
-                continue;
-              used = true;
-              rbra.push_back(bi);
-              rbeg.push_back(base + (int)beg);
-              rcnt.push_back((int)(end - beg));
-              q += (long long)(end - beg);
-              pq += (long long)c->hpairs[bi].nprim * (gprim[end] - gprim[beg]);
-            }
-            if (used) kets.insert(kets.end(), g.begin(), g.end());
+              return lo;
+            };
+            const size_t n_all = std::min(n_order, cnt_ge(tau));
+            if (n_all == 0) continue;
+            cat.rbra.push_back(bi);
+            cat.rall.push_back((int)n_all);
+            cat.r64.push_back((int)std::min(n_all, cnt_ge(tmix)));
           }
-          if (rbra.empty()) continue;
-          Pending P{};
-          P.p.la = la; P.p.lb = lb; P.p.lc = lc; P.p.ld = ld;
-          P.p.prec = (mixed && prec == 1) ? PREC_FP32 : PREC_FP64;
-          P.p.quartets = q;
-          P.p.prim_quartets = pq;
-          P.bra = ints.size();
-          ints.insert(ints.end(), rbra.begin(), rbra.end());
-          P.ket = ints.size();
-          ints.insert(ints.end(), kets.begin(), kets.end());
-          P.beg = ints.size();
-          ints.insert(ints.end(), rbeg.begin(), rbeg.end());
-          P.cnt = ints.size();
-          ints.insert(ints.end(), rcnt.begin(), rcnt.end());
-          // bra primitive slices per row: at most pps primitive pairs per warp
-          P.sl = ints.size();
-          const int pps = for_tensor ? (1 << 30)
-                          : std::max(1, P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
-          std::vector<int> rsl(rbra.size());
-          for (size_t r = 0; r < rbra.size(); ++r) rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + pps - 1) / pps);
-          ints.insert(ints.end(), rsl.begin(), rsl.end());
-          P.off = lls.size();
-          long long acc = 0;
-          for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)rcnt[r] * rsl[r]; }
-          lls.push_back(acc);
-          P.p.cl.nrows = (int)rbra.size();
-          P.p.cl.nlanes = acc;
-          const long long flops = pq * ((long long)vrr + setup_flops(la, lb, lc, ld)) + q * ((long long)hrr + 12LL * neri);
-          P.p.flops = flops;
-          pend.push_back(P);
-          if (P.p.prec == PREC_FP32) {
-            st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
-          } else {
-            st.shell_quartets_fp64 += q; st.prim_quartets_fp64 += pq; st.flops_fp64 += flops;
+          sg.nrow = (int)((long long)cat.rbra.size() - sg.row0);
+          if (sg.nrow == 0) continue;
+          for (int p : g) {
+            cat.kets.push_back(p);
+            cat.kpre.push_back(cat.kpre.back() + c->hpairs[p].nprim);
           }
+          G.segs.push_back(sg);
         }
+        if (!G.segs.empty()) cat.groups.push_back(std::move(G));
       }
     }
   }
-  st.shell_quartets_screened = total_shell_quartets - st.shell_quartets_fp64 - st.shell_quartets_fp32;
+}
+
+// Build the quartet plans of the context's current modes from the catalog.
+int build_plan(fock_ctx* c, bool for_tensor) {
+  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
+  dfree(c->d_plan_int);
+  dfree(c->d_plan_ll);
+  c->plans.clear();
+  if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
+    return FOCK_ERR_INVALID_ARG;
+  const double tau = for_tensor ? 0.0 : c->opt.schwarz_eps;
+  const double tmix = c->opt.mixed_threshold;
+  const bool grouping = c->opt.group_by_contraction != 0;
+  PlanCatalog tensor_cat;
+  if (for_tensor) {
+    build_catalog(c, tau, tmix, grouping, tensor_cat);
+  } else if (!c->catalog.valid || c->catalog.tau != tau || c->catalog.tmix != tmix || c->catalog.grouping != grouping) {
+    build_catalog(c, tau, tmix, grouping, c->catalog);
+    c->catalog.valid = true;
+  }
+  const PlanCatalog& cat = for_tensor ? tensor_cat : c->catalog;
+  const bool ctx_mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
+  // plan state of molecule m (see fock_ctx::mol_mode)
+  auto mode_of = [&](int m) -> int {
+    if (for_tensor || c->mol_mode.empty()) return ctx_mixed ? 1 : 2;
+    return c->mol_mode[m];
+  };
+  bool mixed = false;
+  for (int m = 0; m < c->nmol; ++m) mixed |= mode_of(m) == 1;
+  const bool sharded = !for_tensor && c->opt.shard_count > 1;
+  long long row_counter = 0;  // global row count (shard assignment)
+
+  std::vector<int> ints;
+  std::vector<long long> lls;
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
+  std::vector<Pending> pend;
+  fock_stats st{};
+  st.shell_pairs = (long long)c->hpairs.size();
+  st.prim_pairs = c->nprim_pairs;
+  st.function_quartets_unique = cat.function_quartets_unique;
+  std::vector<int> rbra, rbeg, rcnt, kets, rsl;
+  for (const CatGroup& G : cat.groups) {
+    int hrr = 0, neri = 0;
+    const int vrr = class_vrr_flops(G.la, G.lb, G.lc, G.ld, &hrr, &neri);
+    for (int prec = 0; prec < (mixed ? 2 : 1); ++prec) {
+      rbra.clear(); rbeg.clear(); rcnt.clear(); kets.clear();
+      long long q = 0, pq = 0;
+      for (const CatSeg& sg : G.segs) {
+        const int md = mode_of(sg.mol);
+        if (md == 0 || (prec == 1 && md == 2)) continue;
+        const int base = (int)kets.size();
+        const long long* kp = cat.kpre.data() + sg.ket0;
+        bool used = false;
+        for (long long r = sg.row0; r < sg.row0 + sg.nrow; ++r) {
+          int beg = 0, end = cat.rall[r];
+          if (md == 1) {
+            if (prec == 0) end = cat.r64[r]; else beg = cat.r64[r];
+          }
+          if (end <= beg) continue;
+          // multi-rank build: every shard keeps the rows of its residue class
+          if (sharded && (row_counter++ % c->opt.shard_count) != c->opt.shard_index) continue;
+          used = true;
+          const int bi = cat.rbra[r];
+          rbra.push_back(bi);
+          rbeg.push_back(base + beg);
+          rcnt.push_back(end - beg);
+          q += end - beg;
+          pq += (long long)c->hpairs[bi].nprim * (kp[end] - kp[beg]);
+        }
+        if (used) kets.insert(kets.end(), cat.kets.begin() + sg.ket0, cat.kets.begin() + sg.ket0 + sg.nket);
+      }
+      if (rbra.empty()) continue;
+      Pending P{};
+      P.p.la = G.la; P.p.lb = G.lb; P.p.lc = G.lc; P.p.ld = G.ld;
+      P.p.prec = (mixed && prec == 1) ? PREC_FP32 : PREC_FP64;
+      P.p.quartets = q;
+      P.p.prim_quartets = pq;
+      P.bra = ints.size();
+      ints.insert(ints.end(), rbra.begin(), rbra.end());
+      P.ket = ints.size();
+      ints.insert(ints.end(), kets.begin(), kets.end());
+      P.beg = ints.size();
+      ints.insert(ints.end(), rbeg.begin(), rbeg.end());
+      P.cnt = ints.size();
+      ints.insert(ints.end(), rcnt.begin(), rcnt.end());
+      // bra primitive slices per row: at most pps primitive pairs per warp
+      P.sl = ints.size();
+      const int pps = for_tensor ? (1 << 30)
+                      : std::max(1, P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
+      rsl.resize(rbra.size());
+      for (size_t r = 0; r < rbra.size(); ++r) rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + pps - 1) / pps);
+      ints.insert(ints.end(), rsl.begin(), rsl.end());
+      P.off = lls.size();
+      long long acc = 0;
+      for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)rcnt[r] * rsl[r]; }
+      lls.push_back(acc);
+      P.p.cl.nrows = (int)rbra.size();
+      P.p.cl.nlanes = acc;
+      const long long flops =
+          pq * ((long long)vrr + setup_flops(G.la, G.lb, G.lc, G.ld)) + q * ((long long)hrr + 12LL * neri);
+      P.p.flops = flops;
+      pend.push_back(P);
+      if (P.p.prec == PREC_FP32) {
+        st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
+      } else {
+        st.shell_quartets_fp64 += q; st.prim_quartets_fp64 += pq; st.flops_fp64 += flops;
+      }
+    }
+  }
+  st.shell_quartets_screened = cat.total_shell_quartets - st.shell_quartets_fp64 - st.shell_quartets_fp32;
   // work-queue counters of persistent launches live after the row offsets
   c->queue_base = lls.size();
   lls.insert(lls.end(), pend.size() + 1, 0LL);
@@ -1785,7 +1863,13 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     done[k] = 1;
     ++ndone;
   };
+  // FOCK_GB300_TRACE=1: per-phase host wall times of this SCF on stderr
+  const bool trace = std::getenv("FOCK_GB300_TRACE") != nullptr;
+  using clk = std::chrono::steady_clock;
+  double t_iter = 0.0, t_replan = 0.0;
+  const auto t_loop0 = clk::now();
   for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
+    const auto ti0 = clk::now();
     cudaEventRecord(ev0, s);
     { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
@@ -1861,13 +1945,25 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
         else if (ready[k]) { mode[k] = 2; ready[k] = 0; }
       }
       c->mol_mode = mode;
+      const auto tr0 = clk::now();
       int r = build_plan(c, false);
+      t_replan += std::chrono::duration<double>(clk::now() - tr0).count();
       if (r != FOCK_OK) { fail = r; break; }
       ++replans;
+      if (trace)
+        std::fprintf(stderr, "fock_batch_scf: iter %d re-plan: %d in plan, %d mixed, %d done, %lld quartets\n", iter,
+                     n_in - n_stale, n_mixed - n_ready, ndone,
+                     (long long)(c->stats.shell_quartets_fp64 + c->stats.shell_quartets_fp32));
     }
     for (int k = 0; k < nmol; ++k) eprev[k] = he[k];
     std::swap(Dm, Dn);
+    t_iter += std::chrono::duration<double>(clk::now() - ti0).count();
   }
+  if (trace)
+    std::fprintf(stderr,
+                 "fock_batch_scf: set-up %.3f s; %d builds, iterations %.3f s (Fock builds %.3f s, re-plans %d %.3f s)\n",
+                 std::chrono::duration<double>(t_loop0 - t_start).count(), builds, t_iter, fock_ms * 1e-3, replans,
+                 t_replan);
   if (replans) {  // back to the context's own plan
     c->mol_mode.clear();
     int r = build_plan(c, false);

@@ -47,6 +47,7 @@ class ShardedFock:
         self.rank, self.world, self.group = rank, world, group
         self.ctx = FockContext(atoms, shard_index=rank, shard_count=world, **kw)
         self.n = self.ctx.n
+        self._stream = None
         backend = dist.get_backend(group) if dist.is_available() and dist.is_initialized() else "gloo"
         self._reduce_device = torch.device("cuda", torch.cuda.current_device()) if backend == "nccl" \
             else torch.device("cpu")
@@ -64,8 +65,15 @@ class ShardedFock:
         for t in (D, G):
             if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous() or t.shape != (self.n, self.n):
                 raise ValueError("D and G must be contiguous %d x %d float64 CUDA tensors" % (self.n, self.n))
-        self.ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+        # the build runs on a stream of this object, ordered after and before
+        # the caller's current stream (the library's own stream would not be)
+        cur = torch.cuda.current_stream()
+        if self._stream is None:
+            self._stream = torch.cuda.Stream()
+            self.ctx.set_stream(self._stream.cuda_stream)
+        self._stream.wait_stream(cur)
         self.ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+        cur.wait_stream(self._stream)
         if self._reduce_device.type == "cuda":
             return reduce_partial_g(G, self.group)
         Gh = reduce_partial_g(G.cpu(), self.group)
