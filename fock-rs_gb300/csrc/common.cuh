@@ -58,9 +58,11 @@ struct __align__(16) PrimPair32 {
 // Exponent-sum table: every primitive pair carries the id of its exponent
 // sum p among the distinct sums of the basis; entry (i, j) holds the
 // quantities of a primitive quartet that depend only on p_i and q_j:
-// {(p+q)^(-1/2), 1/(p+q), q/(p+q) = rho/p, p/(p+q) = rho/q}.
-struct __align__(32) ExpPair64 {
-  double rs, inv, rp, rq;
+// {(p+q)^(-1/2), 1/(2(p+q)), q/(p+q) = rho/p, p/(p+q) = rho/q, rho = pq/(p+q)}
+// (FP64: precomputed so that the inner loop spends no FP64 instruction on
+// them; FP32 keeps the 16-byte form {rs, 1/(p+q), rho/p, rho/q}).
+struct __align__(16) ExpPair64 {
+  double rs, o2pq, rp, rq, rho, pad;
 };
 struct __align__(16) ExpPair32 {
   float rs, inv, rp, rq;
@@ -87,6 +89,15 @@ struct ClassLaunch {
   int block;                     // threads per block (0: default)
   int persist_blocks;            // > 0: persistent launch with this many blocks
   unsigned long long* queue;     // work-queue counter of the persistent launch
+  // Optional copy of the ket primitive pairs of this launch, primitive-major
+  // and coalesced: plane c (one 16-byte component of the record: five double2
+  // for FP64, three float4 for FP32) of ket primitive ik of ket list position
+  // pos is element (c * kprim_n + ik) * kcount + pos.  Every ket of the launch
+  // has kprim_n primitive pairs; lanes of one row read consecutive positions.
+  // nullptr: read PrimPair64/PrimPair32 records through the pair's prim_off.
+  const void* kprim;
+  long long kcount;              // length of the launch's ket list
+  int kprim_n;                   // primitive pairs of every ket of the launch
 };
 
 struct EriArgs {
@@ -167,14 +178,23 @@ __device__ __forceinline__ double boys_taylor_row(const double* __restrict__ row
   return f;
 }
 
+// Orders L up to FOCK_BOYS_ROWS_LMAX read one Taylor row per order; higher
+// orders read the row of F_L only and recur downwards with e^{-T}.
+#ifndef FOCK_BOYS_ROWS_LMAX
+#define FOCK_BOYS_ROWS_LMAX 1
+#endif
+
 template <int L>
 __device__ __forceinline__ void boys_scaled(double T, double pref, const double* __restrict__ tab, double* F) {
-  if (T < kBoysTmax) {
-    int i = __float2int_rn(approx_float(T) * (float)kBoysPerUnit);
+  // approx_float truncates, so Tf < 64 exactly when T < 64 (a power of two):
+  // the branch costs a float compare, not an FP64 one
+  const float Tf = approx_float(T);
+  if (Tf < (float)kBoysTmax) {
+    int i = __float2int_rn(Tf * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
     const double d = fma((double)i, -1.0 / kBoysPerUnit, T);
     double ex;
-    if (L <= 1) {
+    if (L <= FOCK_BOYS_ROWS_LMAX) {
 #pragma unroll
       for (int m = 0; m <= L; ++m)
         F[m] = boys_taylor_row(tab + ((size_t)m * kBoysPts + i) * kBoysTerms, d, &ex) * pref;

@@ -31,6 +31,12 @@ constexpr int kEriMaxThreads = 256;
 #define FOCK_KET_UNROLL 2
 #endif
 constexpr int kKetUnroll = FOCK_KET_UNROLL;
+#ifndef FOCK_MINBLOCKS
+#define FOCK_MINBLOCKS 1
+#endif
+#ifndef FOCK_MINBLOCKS_LMAX
+#define FOCK_MINBLOCKS_LMAX 1
+#endif
 
 template <typename R>
 struct PrimLoad;
@@ -39,19 +45,28 @@ template <>
 struct PrimLoad<double> {
   double p, o2p, K, P[3], PA[3];
   int eid;
-  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
-    const double2* v = a.prim64[idx].v;
-    double2 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2), v3 = __ldg(v + 3), v4 = __ldg(v + 4);
+  __device__ __forceinline__ void set(double2 v0, double2 v1, double2 v2, double2 v3, double2 v4) {
     p = v0.x; o2p = v0.y; K = v1.x; P[0] = v1.y; P[1] = v2.x; P[2] = v2.y;
     PA[0] = v3.x; PA[1] = v3.y; PA[2] = v4.x;
     eid = (int)__double_as_longlong(v4.y);
   }
-  // (p+q)^(-1/2), 1/(p+q), rho/p, rho/q for this bra exponent sum and eid_k
-  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, double& rs, double& inv, double& rp,
-                                       double& rq) const {
+  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
+    const double2* v = a.prim64[idx].v;
+    set(__ldg(v), __ldg(v + 1), __ldg(v + 2), __ldg(v + 3), __ldg(v + 4));
+  }
+  // primitive ik of ket list position pos from the launch's coalesced copy
+  __device__ __forceinline__ void load_ket(const ClassLaunch& cl, int ik, long long pos) {
+    const double2* b = static_cast<const double2*>(cl.kprim) + (long long)ik * cl.kcount + pos;
+    const long long plane = (long long)cl.kprim_n * cl.kcount;
+    set(__ldg(b), __ldg(b + plane), __ldg(b + 2 * plane), __ldg(b + 3 * plane), __ldg(b + 4 * plane));
+  }
+  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho for this bra exponent sum and eid_k
+  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, double& rs, double& o2pq, double& rp,
+                                       double& rq, double& rho) const {
     const double2* x = reinterpret_cast<const double2*>(a.xp64 + (size_t)eid * a.nxp + eid_k);
     const double2 x0 = __ldg(x), x1 = __ldg(x + 1);
-    rs = x0.x; inv = x0.y; rp = x1.x; rq = x1.y;
+    rs = x0.x; o2pq = x0.y; rp = x1.x; rq = x1.y;
+    rho = __ldg(reinterpret_cast<const double*>(x + 2));
   }
 };
 
@@ -59,17 +74,25 @@ template <>
 struct PrimLoad<float> {
   float p, o2p, K, P[3], PA[3];
   int eid;
-  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
-    const float4* v = a.prim32[idx].v;
-    float4 v0 = __ldg(v), v1 = __ldg(v + 1), v2 = __ldg(v + 2);
+  __device__ __forceinline__ void set(float4 v0, float4 v1, float4 v2) {
     p = v0.x; o2p = v0.y; K = v0.z; P[0] = v0.w; P[1] = v1.x; P[2] = v1.y;
     PA[0] = v1.z; PA[1] = v1.w; PA[2] = v2.x;
     eid = __float_as_int(v2.y);
   }
-  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, float& rs, float& inv, float& rp,
-                                       float& rq) const {
+  __device__ __forceinline__ void load(const EriArgs& a, int idx) {
+    const float4* v = a.prim32[idx].v;
+    set(__ldg(v), __ldg(v + 1), __ldg(v + 2));
+  }
+  __device__ __forceinline__ void load_ket(const ClassLaunch& cl, int ik, long long pos) {
+    const float4* b = static_cast<const float4*>(cl.kprim) + (long long)ik * cl.kcount + pos;
+    const long long plane = (long long)cl.kprim_n * cl.kcount;
+    set(__ldg(b), __ldg(b + plane), __ldg(b + 2 * plane));
+  }
+  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, float& rs, float& o2pq, float& rp,
+                                       float& rq, float& rho) const {
     const float4 x = __ldg(reinterpret_cast<const float4*>(a.xp32 + (size_t)eid * a.nxp + eid_k));
-    rs = x.x; inv = x.y; rp = x.z; rq = x.w;
+    rs = x.x; o2pq = 0.5f * x.y; rp = x.z; rq = x.w;
+    rho = p * rp;
   }
 };
 
@@ -104,7 +127,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 // Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
 __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, int& bra, int& ket, int& slice,
-                                            int& nslice) {
+                                            int& nslice, long long& pos) {
   int lo = 0, hi = cl.nrows - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -116,7 +139,8 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
   slice = (int)(local / cnt);
   const int k = (int)(local - (long long)slice * cnt);
   bra = __ldg(cl.bra_list + lo);
-  ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
+  pos = (long long)__ldg(cl.row_beg + lo) + k;
+  ket = __ldg(cl.ket_list + pos);
 }
 
 // The work of lane t of a launch (one contracted quartet, one bra slice).
@@ -126,14 +150,16 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   int bra, ket;
   bool active;
   int slice = 0, nslice = 1;
+  long long pos = 0;
   if (MODE == MODE_SCHWARZ) {
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
   } else {
     if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
-    decode_lane(cl, t, bra, ket, slice, nslice);
+    decode_lane(cl, t, bra, ket, slice, nslice, pos);
     active = true;
   }
+  const bool kcoal = MODE != MODE_SCHWARZ && cl.kprim != nullptr;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
   // this warp's slice of the bra primitive pairs
@@ -153,19 +179,18 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
 #pragma unroll kKetUnroll
     for (int ik = 0; ik < nkp; ++ik) {
       PrimLoad<R> kp;
-      kp.load(a, kp0 + ik);
-      R rs, inv, rp, rq;  // (p+q)^(-1/2), 1/(p+q), rho/p, rho/q from the exponent-sum table
-      bp.exps(a, kp.eid, rs, inv, rp, rq);
+      if (kcoal) kp.load_ket(cl, ik, pos); else kp.load(a, kp0 + ik);
+      R rs, o2pq, rp, rq, rho;  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho from the exponent-sum table
+      bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const R r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
-      const R T = bp.p * rp * r2;  // rho |PQ|^2, rho = p q / (p + q)
+      const R T = rho * r2;
       const R pref = bp.K * kp.K * rs;
       R F[L + 1];
       boys_scaled<L>(T, pref, btab, F);
       const R WP[3] = {-rp * PQ[0], -rp * PQ[1], -rp * PQ[2]};
       const R WQ[3] = {rq * PQ[0], rq * PQ[1], rq * PQ[2]};
-      const R o2pq = R(0.5) * inv;
-      C::template vrr<R>(F, bp.PA, WP, kp.PA, WQ, bp.o2p, kp.o2p, o2pq, rp, rq, acc);
+      C::template vrr<R>(F, bp.PA, WP, kp.PA, WQ, PQ, bp.o2p, kp.o2p, o2pq, rp, rq, acc);
     }
   }
 
@@ -305,8 +330,14 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   }
 }
 
+// Resident blocks of kEriMaxThreads asked of the compiler: the s/p classes
+// are latency-bound on their gathers (pair data, exponent-sum table, Boys rows)
+// and gain from more warps per SM, i.e. at most 64 registers a thread.
+template <class C, typename R>
+constexpr int eri_min_blocks() { return (C::L <= FOCK_MINBLOCKS_LMAX) ? FOCK_MINBLOCKS : 1; }
+
 template <class C, typename R, int MODE>
-__global__ void __launch_bounds__(kEriMaxThreads) eri_kernel(const ClassLaunch cl, const EriArgs a) {
+__global__ void __launch_bounds__(kEriMaxThreads, (eri_min_blocks<C, R>())) eri_kernel(const ClassLaunch cl, const EriArgs a) {
   eri_lane<C, R, MODE>(cl, a, (long long)blockIdx.x * blockDim.x + threadIdx.x);
 }
 
@@ -314,7 +345,7 @@ __global__ void __launch_bounds__(kEriMaxThreads) eri_kernel(const ClassLaunch c
 // next 32 lanes of the launch from the launch's work queue (an atomic counter
 // cleared before every build) until the queue is empty.
 template <class C, typename R>
-__global__ void __launch_bounds__(kEriMaxThreads) eri_kernel_persistent(const ClassLaunch cl, const EriArgs a) {
+__global__ void __launch_bounds__(kEriMaxThreads, (eri_min_blocks<C, R>())) eri_kernel_persistent(const ClassLaunch cl, const EriArgs a) {
   const int lane = threadIdx.x & 31;
   const long long nchunks = (cl.nlanes + 31) >> 5;
   for (;;) {
@@ -341,7 +372,8 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cl.nlanes) return;
   int bra, ket, slice, nslice;
-  decode_lane(cl, t, bra, ket, slice, nslice);
+  long long pos;  // the gradient reads ket primitives through prim_off
+  decode_lane(cl, t, bra, ket, slice, nslice, pos);
   const bool active = true;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
@@ -368,17 +400,17 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
       PrimLoad<double> kp;
       kp.load(a, Pk.prim_off + ik);
       const double wc = 2.0 * __ldg(&a.prim64[Pk.prim_off + ik].v[5].x);
-      double rs, inv, rp, rq;
-      bp.exps(a, kp.eid, rs, inv, rp, rq);
+      double rs, o2pq, rp, rq, rho;
+      bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
       const double PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const double r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
-      const double T = bp.p * rp * r2;
+      const double T = rho * r2;
       const double pref = bp.K * kp.K * rs;
       double F[LG + 1];
       boys_scaled<LG>(T, pref, a.boys64, F);
       const double WP[3] = {-rp * PQ[0], -rp * PQ[1], -rp * PQ[2]};
       const double WQ[3] = {rq * PQ[0], rq * PQ[1], rq * PQ[2]};
-      C::template vrr_grad<double>(F, bp.PA, WP, kp.PA, WQ, bp.o2p, kp.o2p, 0.5 * inv, rp, rq, wa, wb, wc, acc0, accA,
+      C::template vrr_grad<double>(F, bp.PA, WP, kp.PA, WQ, bp.o2p, kp.o2p, o2pq, rp, rq, wa, wb, wc, acc0, accA,
                                    accB, accC);
     }
   }

@@ -159,6 +159,7 @@ struct CatSeg {
 };
 struct CatGroup {  // one launch group: bra class, ket class, ket primitive-pair count
   int la, lb, lc, ld;
+  int key;  // primitive pairs of every ket of the group (-1: mixed counts)
   std::vector<CatSeg> segs;
 };
 struct PlanCatalog {
@@ -206,6 +207,7 @@ struct fock_ctx {
   int* d_plan_int = nullptr;
   size_t queue_base = 0;  // first work-queue counter in d_plan_ll
   long long* d_plan_ll = nullptr;
+  unsigned char* d_kprim = nullptr;  // coalesced ket primitive copies of the launches
   fock_stats stats{};
   // molecules (one for fock_ctx_create, many for a batch)
   int nmol = 1;
@@ -295,6 +297,44 @@ long long setup_flops(int la, int lb, int lc, int ld) {
 
 int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
 
+// Copy the primitive pairs of a launch's kets (every ket with nk primitive
+// pairs) into primitive-major planes: element (c * nk + ik) * K + pos holds
+// 16-byte component c of primitive ik of the ket at list position pos.
+__global__ void gather_ket_prims64_kernel(const int* kets, long long K, int nk, const PairInfo* pairs,
+                                          const PrimPair64* prim, double2* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= K * nk) return;
+  const int ik = (int)(t / K);
+  const long long pos = t - (long long)ik * K;
+  const PrimPair64& r = prim[pairs[kets[pos]].prim_off + ik];
+  const long long plane = K * nk;
+#pragma unroll
+  for (int q = 0; q < 5; ++q) out[q * plane + t] = r.v[q];
+}
+__global__ void gather_ket_prims32_kernel(const int* kets, long long K, int nk, const PairInfo* pairs,
+                                          const PrimPair32* prim, float4* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= K * nk) return;
+  const int ik = (int)(t / K);
+  const long long pos = t - (long long)ik * K;
+  const PrimPair32& r = prim[pairs[kets[pos]].prim_off + ik];
+  const long long plane = K * nk;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) out[q * plane + t] = r.v[q];
+}
+static cudaError_t gather_ket_prims(fock_ctx* c, const int* d_kets, long long K, int nk, int prec, unsigned char* out) {
+  const long long n = K * nk;
+  const unsigned blocks = (unsigned)((n + 255) / 256);
+  if (prec == PREC_FP32)
+    gather_ket_prims32_kernel<<<blocks, 256, 0, c->stream>>>(d_kets, K, nk, c->d_pairs, c->d_prim32,
+                                                             reinterpret_cast<float4*>(out));
+  else
+    gather_ket_prims64_kernel<<<blocks, 256, 0, c->stream>>>(d_kets, K, nk, c->d_pairs, c->d_prim64,
+                                                             reinterpret_cast<double2*>(out));
+  c->launches++;
+  return cudaGetLastError();
+}
+
 // Every screened shell-pair row of every launch group, independent of the
 // per-molecule modes and the shard: built once per (Schwarz threshold, mixed
 // threshold, grouping) and re-assembled into launch plans by build_plan, so
@@ -354,6 +394,7 @@ static void build_catalog(const fock_ctx* c, double tau, double tmix, bool group
       for (int key : keys) {
         CatGroup G;
         G.la = la; G.lb = lb; G.lc = lc; G.ld = ld;
+        G.key = key;
         for (int m = 0; m < nmol; ++m) {
           const std::vector<int>& bras = cls[m][X];
           if (bras.empty() || cls[m][Y].empty()) continue;
@@ -411,6 +452,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
   dfree(c->d_plan_int);
   dfree(c->d_plan_ll);
+  dfree(c->d_kprim);
   c->plans.clear();
   if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
     return FOCK_ERR_INVALID_ARG;
@@ -438,7 +480,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
 
   std::vector<int> ints;
   std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; int key; long long nket; };
   std::vector<Pending> pend;
   fock_stats st{};
   st.shell_pairs = (long long)c->hpairs.size();
@@ -485,16 +527,27 @@ int build_plan(fock_ctx* c, bool for_tensor) {
       ints.insert(ints.end(), rbra.begin(), rbra.end());
       P.ket = ints.size();
       ints.insert(ints.end(), kets.begin(), kets.end());
+      P.key = G.key;
+      P.nket = (long long)kets.size();
       P.beg = ints.size();
       ints.insert(ints.end(), rbeg.begin(), rbeg.end());
       P.cnt = ints.size();
       ints.insert(ints.end(), rcnt.begin(), rcnt.end());
       // bra primitive slices per row: at most pps primitive pairs per warp
       P.sl = ints.size();
+      // > 0: bra primitive pairs per lane; < 0: about -pps primitive quartets per lane
+      // (bra primitive pairs per lane = ceil(-pps / ket primitive pairs of the row))
       const int pps = for_tensor ? (1 << 30)
-                      : std::max(1, P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
+                      : (P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
       rsl.resize(rbra.size());
-      for (size_t r = 0; r < rbra.size(); ++r) rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + pps - 1) / pps);
+      for (size_t r = 0; r < rbra.size(); ++r) {
+        int per = std::max(1, pps);
+        if (pps < 0) {
+          const int nk = std::max(1, c->hpairs[kets[rbeg[r]]].nprim);
+          per = std::max(1, (-pps + nk - 1) / nk);
+        }
+        rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + per - 1) / per);
+      }
       ints.insert(ints.end(), rsl.begin(), rsl.end());
       P.off = lls.size();
       long long acc = 0;
@@ -521,7 +574,28 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   CK(dalloc(&c->d_plan_ll, lls.size()));
   if (!ints.empty()) CK(cudaMemcpy(c->d_plan_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (!lls.empty()) CK(cudaMemcpy(c->d_plan_ll, lls.data(), lls.size() * sizeof(long long), cudaMemcpyHostToDevice));
-  for (auto& P : pend) {
+  // coalesced ket primitive copies (launches whose kets share one primitive-pair count)
+  std::vector<size_t> koff(pend.size(), 0);
+  size_t kbytes = 0;
+  for (size_t i = 0; i < pend.size(); ++i) {
+    if (pend[i].key <= 0) continue;
+    koff[i] = kbytes;
+    kbytes += (size_t)pend[i].nket * pend[i].key * (pend[i].p.prec == PREC_FP32 ? 48 : 80);
+  }
+  if (kbytes) {
+    CK(dalloc(&c->d_kprim, kbytes));
+    for (size_t i = 0; i < pend.size(); ++i) {
+      if (pend[i].key <= 0) continue;
+      CK(gather_ket_prims(c, c->d_plan_int + pend[i].ket, pend[i].nket, pend[i].key, pend[i].p.prec,
+                          c->d_kprim + koff[i]));
+    }
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  for (size_t i = 0; i < pend.size(); ++i) {
+    Pending& P = pend[i];
+    P.p.cl.kprim = P.key > 0 ? c->d_kprim + koff[i] : nullptr;
+    P.p.cl.kcount = P.nket;
+    P.p.cl.kprim_n = P.key;
     P.p.cl.bra_list = c->d_plan_int + P.bra;
     P.p.cl.ket_list = c->d_plan_int + P.ket;
     P.p.cl.row_beg = c->d_plan_int + P.beg;
@@ -627,8 +701,8 @@ void fock_options_default(fock_options* o) {
   o->diis_start = 5;
   o->energy_mode = 0;
   o->final_fp64 = 1;
-  o->prims_per_slice = 1;
-  o->prims_per_slice_fp32 = 4;
+  o->prims_per_slice = -4;        // about 4 primitive quartets per lane
+  o->prims_per_slice_fp32 = -32;
   o->block_threads = 128;
   o->persistent = 0;
   o->shard_index = 0;
@@ -677,7 +751,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
   dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64); dfree(c->d_xp32);
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
-  dfree(c->d_plan_int); dfree(c->d_plan_ll);
+  dfree(c->d_plan_int); dfree(c->d_plan_ll); dfree(c->d_kprim);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
   dfree(c->d_mol_off); dfree(c->d_mol_n);
   dfree(c->d_tensor);
@@ -851,10 +925,12 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       const long double p = psum[i], q = psum[j], s = p + q;
       ExpPair64& e = xp64[(size_t)i * c->nxp + j];
       e.rs = (double)(1.0L / sqrtl(s));
-      e.inv = (double)(1.0L / s);
+      e.o2pq = (double)(0.5L / s);
       e.rp = (double)(q / s);
       e.rq = (double)(p / s);
-      xp32[(size_t)i * c->nxp + j] = ExpPair32{(float)e.rs, (float)e.inv, (float)e.rp, (float)e.rq};
+      e.rho = (double)(p * q / s);
+      e.pad = 0.0;
+      xp32[(size_t)i * c->nxp + j] = ExpPair32{(float)e.rs, (float)(1.0L / s), (float)e.rp, (float)e.rq};
     }
   const int npairs = (int)c->hpairs.size();
   const size_t nn = (size_t)c->total_elems;  // all molecule blocks
@@ -1071,7 +1147,8 @@ int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best)
     c->opt.persistent = t.persistent;
   };
   int rc = measure(&cur.ms);
-  const std::vector<int> pps64 = {1, 2, 4}, pps32 = {1, 2, 4, 8}, blk = {64, 128, 256}, per = {0, 1};
+  const std::vector<int> pps64 = {1, 2, 4, -8, -16, -32}, pps32 = {1, 2, 4, 8, -16, -32, -64}, blk = {64, 128, 256},
+                         per = {0, 1};
   for (int dim = 0; dim < 4 && rc == FOCK_OK; ++dim) {
     const std::vector<int>& cand = dim == 0 ? pps64 : dim == 1 ? pps32 : dim == 2 ? blk : per;
     if (dim == 1 && !mixed) continue;
@@ -1099,7 +1176,7 @@ int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best)
 }
 
 int fock_set_tuning(fock_ctx* c, const fock_tuning* t) {
-  if (!c || !t || t->prims_per_slice < 1 || t->prims_per_slice_fp32 < 1 || t->block_threads < 32 ||
+  if (!c || !t || t->prims_per_slice == 0 || t->prims_per_slice_fp32 == 0 || t->block_threads < 32 ||
       t->block_threads > 256 || (t->block_threads & 31))
     return FOCK_ERR_INVALID_ARG;
   c->opt.prims_per_slice = t->prims_per_slice;
@@ -1186,9 +1263,11 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       std::vector<Plan> keep_plans = c->plans;
       int* keep_i = c->d_plan_int;
       long long* keep_l = c->d_plan_ll;
+      unsigned char* keep_k = c->d_kprim;
       const size_t keep_q = c->queue_base;
       c->d_plan_int = nullptr;
       c->d_plan_ll = nullptr;
+      c->d_kprim = nullptr;
       rc = build_plan(c, true);
       if (rc == FOCK_OK) {
         EriArgs a = eri_args(c);
@@ -1202,8 +1281,10 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       }
       dfree(c->d_plan_int);
       dfree(c->d_plan_ll);
+      dfree(c->d_kprim);
       c->d_plan_int = keep_i;
       c->d_plan_ll = keep_l;
+      c->d_kprim = keep_k;
       c->queue_base = keep_q;
       c->plans = keep_plans;
       c->opt = keep;

@@ -151,6 +151,10 @@ def gen_vrr(la, lb, lc, ld):
                 acc_lines.append("    acc[%d] = fma(%s, %s, acc[%d]);" % (j, cf, op, j))
         else:
             acc_lines.append("    acc[%d] += %s;" % (j, v))
+    if L == 1:
+        # (ps|ss): WP_i F_1 = PQ_i (-rp F_1); one multiply instead of forming WP (three)
+        acc_lines = [ln.replace("fma(WP[", "fma(PQ[").replace("], F[1], ", "], nrpF1, ") for ln in acc_lines]
+        acc_lines.insert(0, "    const R nrpF1 = -rp * F[1];")
     E.lines.extend(acc_lines)
     return E, len(es), nf, L
 
@@ -448,8 +452,8 @@ def main(outdir, lmax):
         hdr.append("  static constexpr int NA = %d, NB = %d, NC = %d, ND = %d;" % (ncart(la), ncart(lb), ncart(lc), ncart(ld)))
         hdr.append("  template <typename R>")
         hdr.append("  __device__ __forceinline__ static void vrr(const R* __restrict__ F, const R* PA, const R* WP, const R* QC, const R* WQ,")
-        hdr.append("                                             R o2p, R o2q, R o2pq, R rp, R rq, R* acc) {")
-        hdr.append("    (void)PA; (void)WP; (void)QC; (void)WQ; (void)o2p; (void)o2q; (void)o2pq; (void)rp; (void)rq;")
+        hdr.append("                                             const R* PQ, R o2p, R o2q, R o2pq, R rp, R rq, R* acc) {")
+        hdr.append("    (void)PA; (void)WP; (void)QC; (void)WQ; (void)PQ; (void)o2p; (void)o2q; (void)o2pq; (void)rp; (void)rq;")
         hdr.extend(V.lines)
         hdr.append("  }")
         hdr.append("  template <typename R>")

@@ -90,7 +90,9 @@ typedef struct {
   int final_fp64;  /* FOCK_PREC_MIXED: finish the SCF with FP64 Fock builds once
                       max|FDS - SDF| < 1e-4, so the energy carries no FP32 error */
   int device;      /* CUDA device ordinal */
-  int prims_per_slice;      /* FP64: bra primitive pairs per warp (more warps per heavy quartet) */
+  int prims_per_slice;      /* FP64 bra slicing: > 0 bra primitive pairs per lane (more lanes per heavy
+                               quartet); < 0 about -prims_per_slice primitive quartets per lane (the bra
+                               slice is sized by the ket's primitive-pair count); 0 is invalid */
   int prims_per_slice_fp32; /* same for FP32 quartets */
   int block_threads;        /* threads per block of the class launches (64, 128, 256) */
   int persistent;           /* 1: persistent class launches fed by per-launch work queues */

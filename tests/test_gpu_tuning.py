@@ -31,7 +31,8 @@ def reference_g(mol):
 
 @pytest.mark.parametrize("kw", [dict(persistent=1), dict(block_threads=64), dict(block_threads=256),
                                 dict(prims_per_slice=4), dict(prims_per_slice=2, persistent=1, block_threads=256),
-                                dict(group_by_contraction=0)])
+                                dict(group_by_contraction=0), dict(prims_per_slice=-16, prims_per_slice_fp32=-32),
+                                dict(prims_per_slice=-8, group_by_contraction=0)])
 def test_launch_parameters_keep_g(gpu_lib, mol, reference_g, kw):
     D, G0 = reference_g
     with FockContext(mol, **kw) as ctx:
@@ -51,7 +52,7 @@ def test_autotune_and_cache(gpu_lib, mol, reference_g, tmp_path):
         first = autotune(ctx, Dd.data_ptr(), reps=2, cache_path=cache)
         assert not first["cached"]
         assert first["block_threads"] in (64, 128, 256)
-        assert first["prims_per_slice"] >= 1 and first["persistent"] in (0, 1)
+        assert first["prims_per_slice"] != 0 and first["persistent"] in (0, 1)
         assert first["ms"] > 0
         G = ctx.build_jk(D)
     with FockContext(mol, sign_convention=L.FOCK_SIGN_STANDARD) as ctx:
