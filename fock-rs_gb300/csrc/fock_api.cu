@@ -1334,6 +1334,58 @@ int fock_one_electron(fock_ctx* c, double* S, double* T, double* V) {
   return FOCK_OK;
 }
 
+int fock_orbital_grid_device(fock_ctx* c, const double* coef, int nvox, double box, double min_coef, float* grid_dev) {
+  if (!c || !coef || !grid_dev || nvox <= 0 || nvox > 2048 || !(box > 0.0) || !(min_coef >= 0.0) || c->nmol != 1)
+    return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  // MolecularOrbitals::new keeps the functions with |c| > MIN_COEFFICIENT_MAGNITUDE
+  // (scf/src/molecular_orbitals.rs:69-86); coefficients to the textbook convention
+  const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
+  std::vector<int> sel;
+  std::vector<double> cs;
+  for (int i = 0; i < c->nbf; ++i) {
+    if (!std::isfinite(coef[i])) return FOCK_ERR_INVALID_ARG;
+    if (std::fabs(coef[i]) > min_coef) {
+      sel.push_back(i);
+      cs.push_back(flip ? coef[i] * c->fsign[i] : coef[i]);
+    }
+  }
+  int* d_sel = nullptr;
+  double* d_cs = nullptr;
+  const int nsel = (int)sel.size();
+  cudaError_t e = dalloc(&d_sel, std::max(1, nsel));
+  if (e == cudaSuccess) e = dalloc(&d_cs, std::max(1, nsel));
+  if (e == cudaSuccess && nsel) e = cudaMemcpyAsync(d_sel, sel.data(), nsel * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && nsel) e = cudaMemcpyAsync(d_cs, cs.data(), nsel * sizeof(double), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) {
+    e = md_orbital_grid(md_basis(c), d_sel, d_cs, nsel, nvox, box, grid_dev, c->stream);
+    c->launches++;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_sel);
+  cudaFree(d_cs);
+  CK(e);
+  return FOCK_OK;
+}
+
+int fock_orbital_grid(fock_ctx* c, const double* coef, int nvox, double box, double min_coef, float* grid) {
+  if (!c || !grid || nvox <= 0 || nvox > 2048) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  const size_t n3 = (size_t)nvox * nvox * nvox;
+  float* d = nullptr;
+  CK(dalloc(&d, n3));
+  int rc = fock_orbital_grid_device(c, coef, nvox, box, min_coef, d);
+  cudaError_t e = cudaSuccess;
+  if (rc == FOCK_OK) {
+    e = cudaMemcpyAsync(grid, d, n3 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  }
+  cudaFree(d);
+  if (rc != FOCK_OK) return rc;
+  CK(e);
+  return FOCK_OK;
+}
+
 int fock_gradient(fock_ctx* c, const double* D, const double* W, double* grad) {
   if (!c || !D || !W || !grad || c->opt.shard_count > 1 || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));

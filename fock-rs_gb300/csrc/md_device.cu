@@ -479,6 +479,48 @@ cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, doubl
   return cudaSuccess;
 }
 
+// Molecular orbital on a cubic grid (volumetric/src/main.rs:100-125,
+// scf/src/molecular_orbitals.rs:37-43, contracted_gaussian.rs:320-331):
+// voxel t = x + N (y + N z) sits at ((x/N - 1/2) box, (y/N - 1/2) box,
+// (z/N - 1/2) box) and holds psi = sum_k c_k phi_k(r) over the selected
+// functions, evaluated in FP64 and stored as float.  Threads take consecutive
+// x (coalesced stores); the function loop is uniform across a warp, so its
+// data are broadcast loads.  Primitives with exponent * |r - A|^2 > 700
+// contribute below 1e-300 and are skipped.
+__global__ void orbital_grid_kernel(MdBasis B, const int* sel, const double* csel, int nsel, int nvox, double box,
+                                    float* out) {
+  const long long n3 = (long long)nvox * nvox * nvox;
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n3) return;
+  const int x = (int)(t % nvox), y = (int)((t / nvox) % nvox), z = (int)(t / ((long long)nvox * nvox));
+  const double r[3] = {((double)x / (double)nvox - 0.5) * box, ((double)y / (double)nvox - 0.5) * box,
+                       ((double)z / (double)nvox - 0.5) * box};
+  double psi = 0.0;
+  for (int k = 0; k < nsel; ++k) {
+    const MdFunc& f = B.funcs[__ldg(sel + k)];
+    const double d[3] = {r[0] - f.c[0], r[1] - f.c[1], r[2] - f.c[2]};
+    const double d2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    double poly = 1.0;
+    for (int a = 0; a < 3; ++a)
+      for (int e = 0; e < f.ang[a]; ++e) poly *= d[a];
+    double radial = 0.0;
+    for (int q = f.p0; q < f.p0 + f.np; ++q) {
+      const double ad2 = __ldg(B.exps + q) * d2;
+      if (ad2 < 700.0) radial += __ldg(B.coefs + q) * exp(-ad2);
+    }
+    psi += __ldg(csel + k) * poly * radial;
+  }
+  out[t] = (float)psi;
+}
+
+cudaError_t md_orbital_grid(const MdBasis& B, const int* sel, const double* csel, int nsel, int nvox, double box,
+                            float* out, cudaStream_t s) {
+  const long long n3 = (long long)nvox * nvox * nvox;
+  const int thr = 256;
+  orbital_grid_kernel<<<(unsigned)((n3 + thr - 1) / thr), thr, 0, s>>>(B, sel, csel, nsel, nvox, box, out);
+  return cudaGetLastError();
+}
+
 cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* G, cudaStream_t s) {
   const int thr = 128;
   g_from_tensor_kernel<<<(n * n + thr - 1) / thr, thr, 0, s>>>(eri, D, n, G);

@@ -36,5 +36,9 @@ cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const dou
                                  const int* func_atom, int flags, const double* D, const double* W, double* grad,
                                  cudaStream_t s);
 cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* G, cudaStream_t s);
+// psi on an nvox^3 grid over [-box/2, box/2)^3 from the functions sel[0..nsel)
+// with coefficients csel (textbook convention), float output
+cudaError_t md_orbital_grid(const MdBasis& B, const int* sel, const double* csel, int nsel, int nvox, double box,
+                            float* out, cudaStream_t s);
 
 }  // namespace fockgb

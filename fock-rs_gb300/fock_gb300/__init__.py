@@ -116,6 +116,26 @@ class FockContext:
     def launch_count(self) -> int:
         return lib().fock_launch_count(self.handle)
 
+    def orbital_grid(self, coef, nvox=200, box=20.0, min_coef=0.05) -> np.ndarray:
+        """One molecular orbital (n coefficients, this context's sign convention) on an
+        nvox^3 grid over [-box/2, box/2)^3 bohr: float32 array indexed [z, y, x]
+        (the reference's volumetric viewer: 200 voxels, box 20, |c| > 0.05)."""
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        if coef.shape != (self.n,):
+            raise ValueError("need %d coefficients" % self.n)
+        out = np.zeros(nvox ** 3, dtype=np.float32)
+        check(lib().fock_orbital_grid(self.handle, _dp(coef), nvox, box, min_coef,
+                                      out.ctypes.data_as(C.POINTER(C.c_float))), "fock_orbital_grid")
+        return out.reshape(nvox, nvox, nvox)
+
+    def orbital_grid_device(self, coef, grid_ptr: int, nvox=200, box=20.0, min_coef=0.05):
+        """As orbital_grid, into nvox^3 floats of device memory at grid_ptr."""
+        coef = np.ascontiguousarray(coef, dtype=np.float64)
+        if coef.shape != (self.n,):
+            raise ValueError("need %d coefficients" % self.n)
+        check(lib().fock_orbital_grid_device(self.handle, _dp(coef), nvox, box, min_coef, C.c_void_p(grid_ptr)),
+              "fock_orbital_grid_device")
+
     def scf(self, charge=0):
         n = self.n
         eps, D, Cm = np.zeros(n), np.zeros((n, n)), np.zeros((n, n))

@@ -108,6 +108,9 @@ def lib():
         L.fock_strerror.argtypes = [C.c_int]
         L.fock_strerror.restype = C.c_char_p
         L.fock_measure_fma_peak.argtypes = [C.c_int, C.c_int, dp]
+        fp = C.POINTER(C.c_float)
+        L.fock_orbital_grid.argtypes = [vp, dp, C.c_int, C.c_double, C.c_double, fp]
+        L.fock_orbital_grid_device.argtypes = [vp, dp, C.c_int, C.c_double, C.c_double, vp]
         _lib = L
     return _lib
 

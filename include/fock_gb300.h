@@ -194,6 +194,21 @@ int fock_gradient(fock_ctx* ctx, const double* D, const double* W, double* grad)
  * density_matrix, coefficient_matrix and orbital_energies were filled. */
 int fock_energy_backward(fock_ctx* ctx, const fock_scf_result* result, double* grad);
 
+/* One molecular orbital on a cubic grid (headless form of the reference's
+ * volumetric viewer: volumetric/src/main.rs:100-125 with
+ * MolecularOrbital::evaluate, scf/src/molecular_orbitals.rs:37-43, and
+ * ContractedGaussian::evaluate, contracted_gaussian.rs:320-331).  coef: the
+ * orbital's n coefficients (one column of the coefficient matrix, in the
+ * context's sign convention); functions with |coef| <= min_coef are left out,
+ * as MolecularOrbitals::new does with MIN_COEFFICIENT_MAGNITUDE = 0.05.
+ * Voxel x + nvox (y + nvox z) holds psi at ((x/nvox - 1/2) box, ...) bohr,
+ * evaluated in FP64 and stored as float (the reference uses nvox = 200,
+ * box = 20).  fock_orbital_grid writes nvox^3 floats to host memory,
+ * fock_orbital_grid_device to device memory. */
+int fock_orbital_grid(fock_ctx* ctx, const double* coef, int nvox, double box, double min_coef, float* grid);
+int fock_orbital_grid_device(fock_ctx* ctx, const double* coef, int nvox, double box, double min_coef,
+                             float* grid_dev);
+
 /* Use an external CUDA stream (cudaStream_t) for all work of this context;
  * NULL restores the context's own stream. */
 int fock_set_stream(fock_ctx* ctx, void* stream);

@@ -699,6 +699,41 @@ int orc_eri_tensor(const orc_basis* b, int flags, double schwarz, double* out) {
   return 0;
 }
 
+// One molecular orbital on a cubic grid, as the reference's volumetric viewer
+// computes it: MolecularOrbitals::new keeps |c| > min_coef
+// (scf/src/molecular_orbitals.rs:69-86), MolecularOrbital::evaluate sums
+// c * phi (:37-43), ContractedGaussian::evaluate folds the primitives with
+// diff = position - at (contracted_gaussian.rs:320-331, so the reference sign
+// convention), and voxel i = x + N (y + N z) sits at (x / N - 0.5) * box
+// (volumetric/src/main.rs:100-125); f64 values stored as f32.
+int orc_orbital_grid(const orc_basis* b, const double* coef, int nvox, double box, double min_coef, float* out) {
+  if (nvox <= 0) return -1;
+  std::vector<Func> fs = load_basis(b);
+  std::vector<int> sel;
+  for (int i = 0; i < (int)fs.size(); ++i)
+    if (std::fabs(coef[i]) > min_coef) sel.push_back(i);
+  const long long n3 = (long long)nvox * nvox * nvox;
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n3; ++i) {
+    const int x = (int)(i % nvox), y = (int)((i / nvox) % nvox), z = (int)(i / ((long long)nvox * nvox));
+    const double at[3] = {((double)x / (double)nvox - 0.5) * box, ((double)y / (double)nvox - 0.5) * box,
+                          ((double)z / (double)nvox - 0.5) * box};
+    double psi = 0.0;
+    for (int k : sel) {
+      const Func& f = fs[k];
+      const double diff[3] = {f.pos[0] - at[0], f.pos[1] - at[1], f.pos[2] - at[2]};
+      const double d2 = diff[0] * diff[0] + diff[1] * diff[1] + diff[2] * diff[2];
+      double acc = 0.0;
+      for (const Prim& P : f.prims)
+        acc += P.coef * powi(diff[0], P.ang[0]) * powi(diff[1], P.ang[1]) * powi(diff[2], P.ang[2]) *
+               std::exp(-P.exp * d2);
+      psi += coef[k] * acc;
+    }
+    out[i] = (float)psi;
+  }
+  return 0;
+}
+
 // Partial G of shard `rank` of `nranks` (outer pair index P % nranks == rank):
 // the sum over all shards is G.
 int orc_jk_shard(const orc_basis* b, const double* D, int flags, double schwarz, int rank, int nranks, double* G) {

@@ -81,6 +81,8 @@ def lib():
         L.orc_eri_tensor.argtypes = [C.POINTER(_Basis), C.c_int, C.c_double, dp]
         L.orc_jk.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_double, dp]
         L.orc_jk_shard.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_double, C.c_int, C.c_int, dp]
+        L.orc_orbital_grid.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_double, C.c_double,
+                                       C.POINTER(C.c_float)]
         L.orc_g_from_tensor.argtypes = [dp, dp, C.c_int, dp]
         L.orc_one_electron.argtypes = [C.POINTER(_Basis), C.c_int, dp, dp, C.c_int, dp, dp, dp]
         L.orc_eig.argtypes = [C.c_int, dp, dp, dp]
@@ -144,6 +146,14 @@ def jk_shard(ob, D, rank, nranks, flags=EXACT, schwarz=-1.0):
     if lib().orc_jk_shard(C.byref(ob.s), _dp(D), flags, schwarz, rank, nranks, _dp(G)) != 0:
         raise ValueError("invalid shard %d of %d" % (rank, nranks))
     return G
+
+
+def orbital_grid(ob, coef, nvox, box=20.0, min_coef=0.05):
+    """psi of one orbital (reference sign convention) on nvox^3 voxels, float32, index [z, y, x]."""
+    coef = np.ascontiguousarray(coef, dtype=np.float64)
+    out = np.zeros(nvox ** 3, dtype=np.float32)
+    lib().orc_orbital_grid(C.byref(ob.s), _dp(coef), nvox, box, min_coef, out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out.reshape(nvox, nvox, nvox)
 
 
 def g_from_tensor(eri4, D):

@@ -162,3 +162,36 @@ def test_energy_rotation_invariance(oracle_lib):
                                  energy_mode=1, schwarz=-1.0)
         e.append(r.total_energy)
     assert abs(e[0] - e[1]) < 1e-9
+
+
+def test_orbital_grid_oracle_vs_numpy(oracle_lib):
+    """orc_orbital_grid against a direct numpy restatement of MolecularOrbital::evaluate
+    (scf/src/molecular_orbitals.rs:37-43) over ContractedGaussian::evaluate
+    (contracted_gaussian.rs:320-331): diff = position - at, per-primitive
+    normalisation of primitives.rs:19-27, |c| > 0.05 filter, voxel positions
+    (i / N - 0.5) * box as in volumetric/src/main.rs:110-117."""
+    atoms = B.build_atoms("6-31G", *M.water_sto3g())
+    ob = oracle_lib.OracleBasis(atoms)
+    rng = np.random.default_rng(1)
+    coef = rng.uniform(-0.3, 0.3, size=ob.n)
+    N, box = 12, 20.0
+    got = oracle_lib.orbital_grid(ob, coef, N, box, 0.05)
+    ax = (np.arange(N) / N - 0.5) * box
+    z, y, x = np.meshgrid(ax, ax, ax, indexing="ij")
+    psi = np.zeros((N, N, N))
+    for f in range(ob.n):
+        if abs(coef[f]) <= 0.05:
+            continue
+        c = ob.center.reshape(-1)[3 * f:3 * f + 3]
+        i, j, k = (int(v) for v in ob.ang.reshape(-1)[3 * f:3 * f + 3])
+        dx, dy, dz = c[0] - x, c[1] - y, c[2] - z
+        d2 = dx * dx + dy * dy + dz * dz
+        val = np.zeros_like(d2)
+        for p in range(ob.off[f], ob.off[f + 1]):
+            a = ob.exps[p]
+            den = math.prod(range(i + 1, 2 * i + 1)) * math.prod(range(j + 1, 2 * j + 1)) * \
+                math.prod(range(k + 1, 2 * k + 1))
+            norm = math.sqrt(math.sqrt((2.0 / math.pi * a) ** 3)) * math.sqrt((8.0 * a) ** (i + j + k) / den)
+            val += ob.coefs[p] * norm * dx ** i * dy ** j * dz ** k * np.exp(-a * d2)
+        psi += coef[f] * val
+    assert np.abs(got - psi.astype(np.float32)).max() <= 1e-6 * np.abs(psi).max()
