@@ -89,15 +89,6 @@ struct ClassLaunch {
   int block;                     // threads per block (0: default)
   int persist_blocks;            // > 0: persistent launch with this many blocks
   unsigned long long* queue;     // work-queue counter of the persistent launch
-  // Optional copy of the ket primitive pairs of this launch, primitive-major
-  // and coalesced: plane c (one 16-byte component of the record: five double2
-  // for FP64, three float4 for FP32) of ket primitive ik of ket list position
-  // pos is element (c * kprim_n + ik) * kcount + pos.  Every ket of the launch
-  // has kprim_n primitive pairs; lanes of one row read consecutive positions.
-  // nullptr: read PrimPair64/PrimPair32 records through the pair's prim_off.
-  const void* kprim;
-  long long kcount;              // length of the launch's ket list
-  int kprim_n;                   // primitive pairs of every ket of the launch
 };
 
 struct EriArgs {

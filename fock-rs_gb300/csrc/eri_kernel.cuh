@@ -54,12 +54,6 @@ struct PrimLoad<double> {
     const double2* v = a.prim64[idx].v;
     set(__ldg(v), __ldg(v + 1), __ldg(v + 2), __ldg(v + 3), __ldg(v + 4));
   }
-  // primitive ik of ket list position pos from the launch's coalesced copy
-  __device__ __forceinline__ void load_ket(const ClassLaunch& cl, int ik, long long pos) {
-    const double2* b = static_cast<const double2*>(cl.kprim) + (long long)ik * cl.kcount + pos;
-    const long long plane = (long long)cl.kprim_n * cl.kcount;
-    set(__ldg(b), __ldg(b + plane), __ldg(b + 2 * plane), __ldg(b + 3 * plane), __ldg(b + 4 * plane));
-  }
   // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho for this bra exponent sum and eid_k
   __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, double& rs, double& o2pq, double& rp,
                                        double& rq, double& rho) const {
@@ -82,11 +76,6 @@ struct PrimLoad<float> {
   __device__ __forceinline__ void load(const EriArgs& a, int idx) {
     const float4* v = a.prim32[idx].v;
     set(__ldg(v), __ldg(v + 1), __ldg(v + 2));
-  }
-  __device__ __forceinline__ void load_ket(const ClassLaunch& cl, int ik, long long pos) {
-    const float4* b = static_cast<const float4*>(cl.kprim) + (long long)ik * cl.kcount + pos;
-    const long long plane = (long long)cl.kprim_n * cl.kcount;
-    set(__ldg(b), __ldg(b + plane), __ldg(b + 2 * plane));
   }
   __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, float& rs, float& o2pq, float& rp,
                                        float& rq, float& rho) const {
@@ -127,7 +116,7 @@ __device__ __forceinline__ float warp_sum(float v) {
 
 // Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
 __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, int& bra, int& ket, int& slice,
-                                            int& nslice, long long& pos) {
+                                            int& nslice) {
   int lo = 0, hi = cl.nrows - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -139,8 +128,7 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
   slice = (int)(local / cnt);
   const int k = (int)(local - (long long)slice * cnt);
   bra = __ldg(cl.bra_list + lo);
-  pos = (long long)__ldg(cl.row_beg + lo) + k;
-  ket = __ldg(cl.ket_list + pos);
+  ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
 }
 
 // The work of lane t of a launch (one contracted quartet, one bra slice).
@@ -150,16 +138,14 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   int bra, ket;
   bool active;
   int slice = 0, nslice = 1;
-  long long pos = 0;
   if (MODE == MODE_SCHWARZ) {
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
   } else {
     if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
-    decode_lane(cl, t, bra, ket, slice, nslice, pos);
+    decode_lane(cl, t, bra, ket, slice, nslice);
     active = true;
   }
-  const bool kcoal = MODE != MODE_SCHWARZ && cl.kprim != nullptr;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];
   // this warp's slice of the bra primitive pairs
@@ -179,7 +165,7 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
 #pragma unroll kKetUnroll
     for (int ik = 0; ik < nkp; ++ik) {
       PrimLoad<R> kp;
-      if (kcoal) kp.load_ket(cl, ik, pos); else kp.load(a, kp0 + ik);
+      kp.load(a, kp0 + ik);
       R rs, o2pq, rp, rq, rho;  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho from the exponent-sum table
       bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
@@ -372,8 +358,7 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= cl.nlanes) return;
   int bra, ket, slice, nslice;
-  long long pos;  // the gradient reads ket primitives through prim_off
-  decode_lane(cl, t, bra, ket, slice, nslice, pos);
+  decode_lane(cl, t, bra, ket, slice, nslice);
   const bool active = true;
   const PairInfo& Pb = a.pairs[bra];
   const PairInfo& Pk = a.pairs[ket];

@@ -207,7 +207,6 @@ struct fock_ctx {
   int* d_plan_int = nullptr;
   size_t queue_base = 0;  // first work-queue counter in d_plan_ll
   long long* d_plan_ll = nullptr;
-  unsigned char* d_kprim = nullptr;  // coalesced ket primitive copies of the launches
   fock_stats stats{};
   // molecules (one for fock_ctx_create, many for a batch)
   int nmol = 1;
@@ -296,44 +295,6 @@ long long setup_flops(int la, int lb, int lc, int ld) {
 }
 
 int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
-
-// Copy the primitive pairs of a launch's kets (every ket with nk primitive
-// pairs) into primitive-major planes: element (c * nk + ik) * K + pos holds
-// 16-byte component c of primitive ik of the ket at list position pos.
-__global__ void gather_ket_prims64_kernel(const int* kets, long long K, int nk, const PairInfo* pairs,
-                                          const PrimPair64* prim, double2* out) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= K * nk) return;
-  const int ik = (int)(t / K);
-  const long long pos = t - (long long)ik * K;
-  const PrimPair64& r = prim[pairs[kets[pos]].prim_off + ik];
-  const long long plane = K * nk;
-#pragma unroll
-  for (int q = 0; q < 5; ++q) out[q * plane + t] = r.v[q];
-}
-__global__ void gather_ket_prims32_kernel(const int* kets, long long K, int nk, const PairInfo* pairs,
-                                          const PrimPair32* prim, float4* out) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= K * nk) return;
-  const int ik = (int)(t / K);
-  const long long pos = t - (long long)ik * K;
-  const PrimPair32& r = prim[pairs[kets[pos]].prim_off + ik];
-  const long long plane = K * nk;
-#pragma unroll
-  for (int q = 0; q < 3; ++q) out[q * plane + t] = r.v[q];
-}
-static cudaError_t gather_ket_prims(fock_ctx* c, const int* d_kets, long long K, int nk, int prec, unsigned char* out) {
-  const long long n = K * nk;
-  const unsigned blocks = (unsigned)((n + 255) / 256);
-  if (prec == PREC_FP32)
-    gather_ket_prims32_kernel<<<blocks, 256, 0, c->stream>>>(d_kets, K, nk, c->d_pairs, c->d_prim32,
-                                                             reinterpret_cast<float4*>(out));
-  else
-    gather_ket_prims64_kernel<<<blocks, 256, 0, c->stream>>>(d_kets, K, nk, c->d_pairs, c->d_prim64,
-                                                             reinterpret_cast<double2*>(out));
-  c->launches++;
-  return cudaGetLastError();
-}
 
 // Every screened shell-pair row of every launch group, independent of the
 // per-molecule modes and the shard: built once per (Schwarz threshold, mixed
@@ -452,7 +413,6 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
   dfree(c->d_plan_int);
   dfree(c->d_plan_ll);
-  dfree(c->d_kprim);
   c->plans.clear();
   if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
     return FOCK_ERR_INVALID_ARG;
@@ -480,7 +440,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
 
   std::vector<int> ints;
   std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; int key; long long nket; };
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
   std::vector<Pending> pend;
   fock_stats st{};
   st.shell_pairs = (long long)c->hpairs.size();
@@ -527,8 +487,6 @@ int build_plan(fock_ctx* c, bool for_tensor) {
       ints.insert(ints.end(), rbra.begin(), rbra.end());
       P.ket = ints.size();
       ints.insert(ints.end(), kets.begin(), kets.end());
-      P.key = G.key;
-      P.nket = (long long)kets.size();
       P.beg = ints.size();
       ints.insert(ints.end(), rbeg.begin(), rbeg.end());
       P.cnt = ints.size();
@@ -574,28 +532,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   CK(dalloc(&c->d_plan_ll, lls.size()));
   if (!ints.empty()) CK(cudaMemcpy(c->d_plan_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (!lls.empty()) CK(cudaMemcpy(c->d_plan_ll, lls.data(), lls.size() * sizeof(long long), cudaMemcpyHostToDevice));
-  // coalesced ket primitive copies (launches whose kets share one primitive-pair count)
-  std::vector<size_t> koff(pend.size(), 0);
-  size_t kbytes = 0;
-  for (size_t i = 0; i < pend.size(); ++i) {
-    if (pend[i].key <= 0) continue;
-    koff[i] = kbytes;
-    kbytes += (size_t)pend[i].nket * pend[i].key * (pend[i].p.prec == PREC_FP32 ? 48 : 80);
-  }
-  if (kbytes) {
-    CK(dalloc(&c->d_kprim, kbytes));
-    for (size_t i = 0; i < pend.size(); ++i) {
-      if (pend[i].key <= 0) continue;
-      CK(gather_ket_prims(c, c->d_plan_int + pend[i].ket, pend[i].nket, pend[i].key, pend[i].p.prec,
-                          c->d_kprim + koff[i]));
-    }
-    CK(cudaStreamSynchronize(c->stream));
-  }
   for (size_t i = 0; i < pend.size(); ++i) {
     Pending& P = pend[i];
-    P.p.cl.kprim = P.key > 0 ? c->d_kprim + koff[i] : nullptr;
-    P.p.cl.kcount = P.nket;
-    P.p.cl.kprim_n = P.key;
     P.p.cl.bra_list = c->d_plan_int + P.bra;
     P.p.cl.ket_list = c->d_plan_int + P.ket;
     P.p.cl.row_beg = c->d_plan_int + P.beg;
@@ -751,7 +689,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
   dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64); dfree(c->d_xp32);
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
-  dfree(c->d_plan_int); dfree(c->d_plan_ll); dfree(c->d_kprim);
+  dfree(c->d_plan_int); dfree(c->d_plan_ll);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
   dfree(c->d_mol_off); dfree(c->d_mol_n);
   dfree(c->d_tensor);
@@ -1263,11 +1201,9 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       std::vector<Plan> keep_plans = c->plans;
       int* keep_i = c->d_plan_int;
       long long* keep_l = c->d_plan_ll;
-      unsigned char* keep_k = c->d_kprim;
       const size_t keep_q = c->queue_base;
       c->d_plan_int = nullptr;
       c->d_plan_ll = nullptr;
-      c->d_kprim = nullptr;
       rc = build_plan(c, true);
       if (rc == FOCK_OK) {
         EriArgs a = eri_args(c);
@@ -1281,10 +1217,8 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       }
       dfree(c->d_plan_int);
       dfree(c->d_plan_ll);
-      dfree(c->d_kprim);
       c->d_plan_int = keep_i;
       c->d_plan_ll = keep_l;
-      c->d_kprim = keep_k;
       c->queue_base = keep_q;
       c->plans = keep_plans;
       c->opt = keep;
