@@ -206,6 +206,18 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
                           "launches_per_build": (b.launch_count() - l0) // (steps + warmup)}
         Gs[name] = G.clone()
     res_prec["mixed"]["speedup_vs_fp64"] = res_prec["fp64"]["ms_per_build"] / res_prec["mixed"]["ms_per_build"]
+    # autotuned launch parameters of the mixed batched build (fock_batch_autotune, fresh cache)
+    import tempfile
+    from fock_gb300.tuning import autotune
+    b.set_precision(L.FOCK_PREC_MIXED, F.options().mixed_threshold)
+    with tempfile.TemporaryDirectory() as td:
+        tuned = autotune(b, D.data_ptr(), reps=2, cache_path=os.path.join(td, "tune.json"), batch=True)
+    t = _event_times(torch, stream, lambda: b.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
+    ms_t = sum(t) / len(t)
+    res_prec["mixed_autotuned"] = {"ms_per_build": ms_t, "quartets_per_s": nq / (ms_t * 1e-3),
+                                   "speedup_vs_fp64": res_prec["fp64"]["ms_per_build"] / ms_t,
+                                   "tuning": {k: tuned[k] for k in ("prims_per_slice", "prims_per_slice_fp32",
+                                                                    "block_threads", "persistent")}}
     dG = Gs["mixed"] - Gs["fp64"]
     de = [0.5 * float((D[o:o + n * n] * dG[o:o + n * n]).sum().item()) for o, n in zip(b.offsets, b.nbf)]
     res_prec["mixed"]["max_single_build_energy_error_eh"] = max(abs(x) for x in de)

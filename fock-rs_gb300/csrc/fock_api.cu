@@ -1784,6 +1784,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     runs.push_back({k, e - k, c->mol_nbf[k], nocc[k], c->mol_off[k], woff[k]});
     k = e;
   }
+  std::vector<Run> act = runs;  // the dense algebra's runs (see rebuild_active)
   const int ring = std::max(1, std::min(c->opt.diis_len, 16));
   std::vector<void*> bufs;
   bool ok = true;
@@ -1851,12 +1852,24 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   void* dwork = mk(dws);
   std::vector<char> hwork(std::max<size_t>(hws, 8));
   if (!ok) { if (sp) cusolverDnDestroyParams(sp); cleanup(); return FOCK_ERR_OOM; }
+  const bool trace_syev = std::getenv("FOCK_GB300_TRACE") != nullptr;
+  int syev_calls = 0;
   auto syev = [&](double* A) {  // eigenvectors in place, eigenvalues into w
-    for (const Run& r : runs) {
+    for (const Run& r : act) {
+      const bool sample = trace_syev && (syev_calls % 97) == 0;
+      if (sample) cudaStreamSynchronize(s);
+      const auto t0 = std::chrono::steady_clock::now();
       cks(cusolverDnXsyevBatched(c->solver, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r.n, CUDA_R_64F,
                                  A + r.off, r.n, CUDA_R_64F, w + r.woff, CUDA_R_64F, dwork, dws, hwork.data(), hws,
                                  d_info + r.m0, r.cnt));
       c->launches++;
+      ++syev_calls;
+      if (sample) {
+        cudaStreamSynchronize(s);
+        std::fprintf(stderr, "fock_batch_scf: syev n %d batch %d: %.3f ms (workspace device %zu host %zu)\n", r.n,
+                     r.cnt, 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count(), dws,
+                     hws);
+      }
     }
   };
   // Loewdin X = U diag(w^-1/2) U^T
@@ -1864,13 +1877,13 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   syev(U);
   cku(kb_scale_cols(U, w, d_woff, c->d_mol_off, c->d_mol_n, nmol, T, W, s));
   c->launches++;
-  for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.n, &one, W, U, X);
+  for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.n, &one, W, U, X);
   auto density_from = [&](const double* Fin, double* Dout) {
-    for (const Run& r : runs) gemm(r, CUBLAS_OP_T, CUBLAS_OP_N, r.n, &one, X, Fin, T1);
-    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, X, T2);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_T, CUBLAS_OP_N, r.n, &one, X, Fin, T1);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, X, T2);
     syev(T2);
-    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T2, Cm);
-    for (const Run& r : runs) {
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T2, Cm);
+    for (const Run& r : act) {
       if (r.nocc > 0) {
         gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.nocc, &two, Cm, Cm, Dout);
       } else {
@@ -1902,7 +1915,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     o.nuclear_repulsion = vnn[k];
   }
   std::vector<int> order;
-  int next_slot = 0, builds = 0, ndone = 0, replans = 0;
+  int next_slot = 0, builds = 0, ndone = 0, replans = 0, ndone_act = 0;
   double fock_ms = 0.0;
   cudaEvent_t ev0, ev1;
   cudaEventCreate(&ev0);
@@ -1930,21 +1943,49 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     done[k] = 1;
     ++ndone;
   };
+  // The dense algebra runs over the molecules still iterating: a run whose
+  // molecules are mostly converged splits into its active segments, so frozen
+  // molecules stop costing eigensolves and products.
+  auto rebuild_active = [&]() {
+    act.clear();
+    for (const Run& r : runs) {
+      int nact = 0;
+      for (int k = r.m0; k < r.m0 + r.cnt; ++k) nact += !done[k];
+      if (nact == 0) continue;
+      if (2 * nact >= r.cnt) { act.push_back(r); continue; }
+      for (int k = r.m0; k < r.m0 + r.cnt;) {
+        if (done[k]) { ++k; continue; }
+        int e = k;
+        while (e < r.m0 + r.cnt && !done[e]) ++e;
+        act.push_back({k, e - k, r.n, r.nocc, c->mol_off[k], woff[k]});
+        k = e;
+      }
+    }
+  };
   // FOCK_GB300_TRACE=1: per-phase host wall times of this SCF on stderr
   const bool trace = std::getenv("FOCK_GB300_TRACE") != nullptr;
   using clk = std::chrono::steady_clock;
-  double t_iter = 0.0, t_replan = 0.0;
+  double t_iter = 0.0, t_replan = 0.0, t_ph[4] = {0, 0, 0, 0};
+  auto phase = [&](int k, clk::time_point& t0) {  // traced runs only: device time of one phase
+    if (!trace) return;
+    cudaStreamSynchronize(s);
+    const auto t1 = clk::now();
+    t_ph[k] += std::chrono::duration<double>(t1 - t0).count();
+    t0 = t1;
+  };
   const auto t_loop0 = clk::now();
   for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
     const auto ti0 = clk::now();
+    auto tp = ti0;
     cudaEventRecord(ev0, s);
     { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
     builds++;
+    phase(0, tp);
     cku(k_add(H, G, F, (int)T, s));
     cku(kb_energy(Dm, H, G, c->d_mol_off, nmol, ecur, s));
-    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, F, Dm, T1);
-    for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, F, Dm, T1);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
     const int slot = next_slot;
     next_slot = (next_slot + 1) % ring;
     if ((int)order.size() == ring) order.erase(order.begin());
@@ -1962,14 +2003,16 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       c->launches += 2;
       Fuse = Fd;
     }
+    phase(1, tp);
     if (shift != 0.0) {  // F + b (S - 1/2 S D S), every block
-      for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, S, Dm, T1);
-      for (const Run& r : runs) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
+      for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, S, Dm, T1);
+      for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
       cku(k_level_shift(Fuse, S, T2, shift, T, Fsh, s));
       c->launches++;
       Fuse = Fsh;
     }
     density_from(Fuse, Dn);
+    phase(2, tp);
     cku(kb_energy(Dn, H, G, c->d_mol_off, nmol, eref, s));
     c->launches++;
     cku(cudaMemcpyAsync(he.data(), ecur, nmol * 8, cudaMemcpyDeviceToHost, s));
@@ -2006,6 +2049,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       if (done[k]) ++n_stale;
     }
     if (ndone == nmol) break;
+    if (ndone != ndone_act) { rebuild_active(); ndone_act = ndone; }
     if ((n_mixed > 0 && n_ready == n_mixed) || n_ready + n_stale >= std::max(1, n_in / 4)) {
       for (int k = 0; k < nmol; ++k) {
         if (done[k]) mode[k] = 0;
@@ -2031,6 +2075,9 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
                  "fock_batch_scf: set-up %.3f s; %d builds, iterations %.3f s (Fock builds %.3f s, re-plans %d %.3f s)\n",
                  std::chrono::duration<double>(t_loop0 - t_start).count(), builds, t_iter, fock_ms * 1e-3, replans,
                  t_replan);
+  if (trace)
+    std::fprintf(stderr, "fock_batch_scf: phases: build %.3f s, F/DIIS %.3f s, shift+density %.3f s\n", t_ph[0],
+                 t_ph[1], t_ph[2]);
   if (replans) {  // back to the context's own plan
     c->mol_mode.clear();
     int r = build_plan(c, false);
