@@ -106,9 +106,11 @@ def benzene_atoms():
     return B.build_atoms("6-31G", Zs, xyz)
 
 
-def cpu_reference(steps, warmup, sample_w=3, threads=0):
+def cpu_reference(steps, warmup, threads=0):
     """Reference algorithm on the host cores; one step = the sampled outer-w
-    iterations of from_basis + the full electron_terms and G loops."""
+    iterations of from_basis + the full electron_terms and G loops.  The w
+    loop is the parallel one (rayon in the reference, OpenMP here), so the
+    sample keeps at least 4 w iterations per thread: every core stays busy."""
     import oracle
     oracle.build()
     atoms = benzene_atoms()
@@ -118,7 +120,7 @@ def cpu_reference(steps, warmup, sample_w=3, threads=0):
     Cm = rng.normal(size=(n, 21)) / np.sqrt(n)
     D = 2.0 * Cm @ Cm.T
     nthreads = threads or oracle.max_threads()
-    stride = max(1, n // sample_w)
+    stride = max(1, n // (4 * nthreads))
     rates, tf_all = [], []
     total_unique = WORKLOAD["unique_quartets"]
     for it in range(warmup + steps):
