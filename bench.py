@@ -281,6 +281,21 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
     out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_build"] / out["mixed"]["ms_per_build"]
     out["mixed"]["single_build_energy_error_eh"] = abs(0.5 * float((D * (Gs["mixed"] - Gs["fp64"])).sum().item()))
     ctx.close()
+    # mixed-precision SCF (final iterations FP64) and the nuclear gradient: analytic
+    # derivative kernels for the s/p classes, finite-difference kernels for the d classes
+    with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
+                       energy_mode=1, epsilon=1e-8, max_iters=100, device=local) as sctx:
+        t0 = time.perf_counter()
+        rc, r, _, _, _ = sctx.scf(0)
+        torch.cuda.synchronize()
+        scf_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g = sctx.energy_backward()
+        grad_s = time.perf_counter() - t0
+    out["scf_mixed"] = {"rc": rc, "wall_s": scf_s, "iterations": r.iterations, "energy": r.total_energy,
+                        "converged": bool(r.converged), "fock_builds": r.fock_builds, "fock_s": r.fock_seconds}
+    out["gradient"] = {"wall_s": grad_s, "max_abs": float(np.abs(g).max()),
+                       "net_force": float(np.abs(g.sum(axis=0)).max()), "components": int(g.size)}
     return out
 
 

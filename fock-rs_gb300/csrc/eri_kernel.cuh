@@ -1,14 +1,13 @@
 // ERI + J/K digestion kernel template, one instantiation per angular class.
 //
-// Work mapping (MODE_JK / MODE_TENSOR): one warp = one bra shell pair and up
-// to 32 ket shell pairs of the same (row) list; one lane = one contracted
-// shell quartet.  The bra is uniform across the warp, so its primitive loop
-// has a uniform trip count and its J block is reduced with warp shuffles
-// before a single set of atomics.  Every lane runs Obara-Saika VRR over the
-// bra x ket primitive pairs into contracted [e0|f0] accumulators held in
-// registers, then HRR once per contracted quartet, then digests the
-// integrals straight into the Fock accumulator M (G = M + M^T): the N^4
-// tensor is never stored.
+// Work mapping (MODE_JK / MODE_TENSOR): one lane = one contracted shell
+// quartet and one slice of its bra primitive pairs; lanes are packed densely
+// over the rows of a launch (see ClassLaunch), so a warp's 32 lanes usually
+// share one bra pair and its ket primitive-pair count.  Every lane runs
+// Obara-Saika VRR over its bra x ket primitive pairs into contracted [e0|f0]
+// accumulators held in registers, then HRR once, then digests the integrals
+// straight into the Fock accumulator M (G = M + M^T) with FP64 atomics: the
+// N^4 tensor is never stored.
 //
 // Digestion of one integral v = (ij|kl) with degeneracy factor s (1/2 for
 // each of a==b, c==d, ab==cd) follows from the eight index images of v:
@@ -101,17 +100,6 @@ __device__ __forceinline__ double dens<double>(const EriArgs& a, size_t mo, int 
 template <>
 __device__ __forceinline__ float dens<float>(const EriArgs& a, size_t mo, int ld, int i, int j) {
   return __ldg(a.D32 + mo + (size_t)i * ld + j);
-}
-
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
 }
 
 // Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
@@ -438,36 +426,49 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
   }
 }
 
+// Gradient launch of the classes whose analytic derivative recurrences are
+// not generated (finite-difference kernel, eri_grad_fd.cuh); defined and
+// instantiated in translation units of their own (gen/inst_fd_*.cu).
 template <class C>
-cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
-  if (mode == MODE_GRAD) {
-    if constexpr (C::HAS_GRAD) {
-      if (cl.nlanes <= 0) return cudaSuccess;
-      const long long blocks = (cl.nlanes + kEriThreads - 1) / kEriThreads;
-      if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      eri_grad_kernel<C><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
-      return cudaGetLastError();
-    } else {
-      return cudaErrorNotSupported;
+cudaError_t launch_grad_fd(const ClassLaunch& cl, const EriArgs& a, cudaStream_t s);
+
+// Launch pieces of one class.  The large classes instantiate each piece in a
+// translation unit of its own (gen/inst_*_p<k>.cu, declared extern in
+// gen/inst_*.cu), so that nvcc compiles their kernels in parallel.
+enum LaunchPart { PART_JK64 = 0, PART_JK32 = 1, PART_PERSISTENT = 2, PART_AUX = 3 };
+
+template <class C, int PART>
+cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if constexpr (PART == PART_AUX) {
+    if (mode == MODE_GRAD) {
+      if constexpr (C::HAS_GRAD) {
+        if (cl.nlanes <= 0) return cudaSuccess;
+        const long long blocks = (cl.nlanes + kEriThreads - 1) / kEriThreads;
+        if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+        eri_grad_kernel<C><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
+        return cudaGetLastError();
+      } else {
+        return launch_grad_fd<C>(cl, a, s);
+      }
     }
-  }
-  if (mode == MODE_SCHWARZ) {
-    if (cl.nrows <= 0) return cudaSuccess;
-    if constexpr (C::LA == C::LC && C::LB == C::LD) {
-      const int blocks = (cl.nrows + kEriThreads - 1) / kEriThreads;
-      eri_kernel<C, double, MODE_SCHWARZ><<<blocks, kEriThreads, 0, s>>>(cl, a);
-      return cudaGetLastError();
-    } else {
-      return cudaErrorInvalidValue;
+    if (mode == MODE_SCHWARZ) {
+      if (cl.nrows <= 0) return cudaSuccess;
+      if constexpr (C::LA == C::LC && C::LB == C::LD) {
+        const int blocks = (cl.nrows + kEriThreads - 1) / kEriThreads;
+        eri_kernel<C, double, MODE_SCHWARZ><<<blocks, kEriThreads, 0, s>>>(cl, a);
+        return cudaGetLastError();
+      } else {
+        return cudaErrorInvalidValue;
+      }
     }
   }
   if (cl.nlanes <= 0) return cudaSuccess;
   const int thr = (cl.block >= 32 && cl.block <= kEriMaxThreads) ? cl.block : kEriThreads;
   const long long blocks = (cl.nlanes + thr - 1) / thr;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  if (mode == MODE_TENSOR) {
+  if constexpr (PART == PART_AUX) {
     eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
-  } else if (cl.queue && cl.persist_blocks != 0) {
+  } else if constexpr (PART == PART_PERSISTENT) {
     // persistent: half of the resident capacity of the GPU (other classes run
     // beside it on the other streams of the captured build)
     long long pb = cl.persist_blocks;
@@ -485,12 +486,21 @@ cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int 
     if (pb > blocks) pb = blocks;
     if (prec == PREC_FP32) eri_kernel_persistent<C, float><<<(unsigned)pb, thr, 0, s>>>(cl, a);
     else eri_kernel_persistent<C, double><<<(unsigned)pb, thr, 0, s>>>(cl, a);
-  } else if (prec == PREC_FP32) {
+  } else if constexpr (PART == PART_JK32) {
     eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   } else {
     eri_kernel<C, double, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   }
   return cudaGetLastError();
+}
+
+template <class C>
+cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if (mode == MODE_GRAD || mode == MODE_SCHWARZ || mode == MODE_TENSOR)
+    return launch_part<C, PART_AUX>(cl, a, mode, prec, s);
+  if (cl.queue && cl.persist_blocks != 0) return launch_part<C, PART_PERSISTENT>(cl, a, mode, prec, s);
+  if (prec == PREC_FP32) return launch_part<C, PART_JK32>(cl, a, mode, prec, s);
+  return launch_part<C, PART_JK64>(cl, a, mode, prec, s);
 }
 
 }  // namespace fockgb

@@ -1324,8 +1324,6 @@ int fock_gradient(fock_ctx* c, const double* D, const double* W, double* grad) {
   if (!c || !D || !W || !grad || c->opt.shard_count > 1 || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
   if (c->opt.eri_mode != FOCK_ERI_EXACT) return FOCK_ERR_INVALID_ARG;
-  for (const HostShell& h : c->shells)
-    if (h.l > kGeneratedGradLmax) return FOCK_ERR_UNSUPPORTED_L;
   const int n = c->nbf, na = c->natom;
   const size_t nn = (size_t)n * n;
   std::vector<double> Ds(nn), Ws(nn);

@@ -431,6 +431,7 @@ def quartet_classes(lmax):
 
 
 GRAD_LMAX = 1  # gradient recurrences are generated for classes with every l <= GRAD_LMAX
+SPLIT_L = 5  # classes with la+lb+lc+ld >= SPLIT_L compile in four units each
 
 
 def main(outdir, lmax):
@@ -501,13 +502,35 @@ def main(outdir, lmax):
     for (la, lb, lc, ld) in classes:
         name = "Cls_%d_%d_%d_%d" % (la, lb, lc, ld)
         names.append(name)
+        # the large classes compile their four launch pieces in units of their own
+        split = la + lb + lc + ld >= SPLIT_L
+        sig = "(const ClassLaunch&, const EriArgs&, int, int, cudaStream_t)"
         with open(os.path.join(outdir, "inst_%d%d%d%d.cu" % (la, lb, lc, ld)), "w") as f:
             f.write('// Generated by gen_eri.py. Do not edit.\n#include "cls_%d%d%d%d.cuh"\n#include "../eri_kernel.cuh"\n'
                     % (la, lb, lc, ld))
             f.write("namespace fockgb {\n")
+            if split:
+                for part in range(4):
+                    f.write("extern template cudaError_t launch_part<%s, %d>%s;\n" % (name, part, sig))
             f.write("cudaError_t launch_%s(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {\n" % name)
             f.write("  return launch_class<%s>(cl, a, mode, prec, s);\n}\n" % name)
             f.write("}  // namespace fockgb\n")
+        if split:
+            for part in range(4):
+                with open(os.path.join(outdir, "inst_%d%d%d%d_p%d.cu" % (la, lb, lc, ld, part)), "w") as f:
+                    f.write('// Generated by gen_eri.py. Do not edit.\n#include "cls_%d%d%d%d.cuh"\n'
+                            '#include "../eri_kernel.cuh"\n' % (la, lb, lc, ld))
+                    f.write("namespace fockgb {\ntemplate cudaError_t launch_part<%s, %d>%s;\n}  // namespace fockgb\n"
+                            % (name, part, sig))
+        if max(la, lb, lc, ld) > GRAD_LMAX:
+            # finite-difference gradient kernel of the class, in a unit of its own
+            with open(os.path.join(outdir, "inst_fd_%d%d%d%d.cu" % (la, lb, lc, ld)), "w") as f:
+                f.write('// Generated by gen_eri.py. Do not edit.\n#include "cls_%d%d%d%d.cuh"\n'
+                        '#include "../eri_grad_fd.cuh"\n' % (la, lb, lc, ld))
+                f.write("namespace fockgb {\n")
+                f.write("template cudaError_t launch_grad_fd<%s>(const ClassLaunch&, const EriArgs&, cudaStream_t);\n"
+                        % name)
+                f.write("}  // namespace fockgb\n")
     with open(os.path.join(outdir, "dispatch.cuh"), "w") as f:
         f.write("// Generated by gen_eri.py. Do not edit.\n#pragma once\nnamespace fockgb {\n")
         for n in names:
