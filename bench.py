@@ -284,7 +284,8 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
     # mixed-precision SCF (final iterations FP64) and the nuclear gradient: analytic
     # derivative kernels for the s/p classes, finite-difference kernels for the d classes
     with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
-                       energy_mode=1, epsilon=1e-8, max_iters=100, device=local) as sctx:
+                       energy_mode=1, epsilon=1e-8, max_iters=100, level_shift=BATCH_LEVEL_SHIFT,
+                       device=local) as sctx:
         t0 = time.perf_counter()
         rc, r, _, _, _ = sctx.scf(0)
         torch.cuda.synchronize()
@@ -293,6 +294,7 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
         g = sctx.energy_backward()
         grad_s = time.perf_counter() - t0
     out["scf_mixed"] = {"rc": rc, "wall_s": scf_s, "iterations": r.iterations, "energy": r.total_energy,
+                        "level_shift_eh": BATCH_LEVEL_SHIFT, "energy_per_water": r.total_energy / 32,
                         "converged": bool(r.converged), "fock_builds": r.fock_builds, "fock_s": r.fock_seconds}
     out["gradient"] = {"wall_s": grad_s, "max_abs": float(np.abs(g).max()),
                        "net_force": float(np.abs(g.sum(axis=0)).max()), "components": int(g.size)}
