@@ -185,9 +185,11 @@ int fock_scf(fock_ctx* ctx, int charge, fock_scf_result* result);
  *   dE/dX = sum D dH/dX - sum W dS/dX + sum_unique 4 s Gam (ij|kl)^X + dVnn/dX
  * with Gam_ijkl = D_ij D_kl - (D_ik D_jl + D_il D_jk)/4 and the energy-weighted
  * density W = 2 sum_occ eps_k C_ik C_jk.  The derivative ERIs are formed and
- * contracted on the fly (fused kernel, no N^4 storage).  D, W: host row-major
- * n_basis^2 in the selected sign convention; grad: 3*natom, hartree/bohr,
- * atom-major (x, y, z).  Exact ERI mode, shells with l <= 1. */
+ * contracted on the fly (fused kernels, no N^4 storage): analytically for
+ * quartets of s and p shells, by a fourth-order central difference of the
+ * quartet's integrals in the centres (step 2e-4 bohr) for quartets with a d
+ * shell.  D, W: host row-major n_basis^2 in the selected sign convention;
+ * grad: 3*natom, hartree/bohr, atom-major (x, y, z).  Exact ERI mode only. */
 int fock_gradient(fock_ctx* ctx, const double* D, const double* W, double* grad);
 
 /* Backward of fock_scf's energy: the gradient at a converged result whose
