@@ -1412,6 +1412,12 @@ int fock_measure_fma_peak(int device, int fp64, double* gflops) {
 // ---------------------------------------------------------------------------
 // RHF (scf/src/lib.rs:73-258) on the device.  Column-major n x n buffers.
 // ---------------------------------------------------------------------------
+// The level shift is applied in full while the previous iteration's DIIS error
+// max|FDS - SDF| is above kShiftFade and in proportion to that error below it,
+// so that the final iterations are plain DIIS (the self-consistent solution
+// does not depend on the shift).
+constexpr double kShiftFade = 1e-1;
+
 int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   if (!c || !res || c->opt.shard_count > 1 || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
@@ -1522,6 +1528,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   std::vector<int> order;  // slots, oldest first
   int next_slot = 0;
   double e_prev = 0.0;
+  double err_prev = 1.0, shift_now = 0.0;  // previous DIIS error; shift of this iteration
   double fock_ms = 0.0;
   int builds = 0;
   cudaEvent_t ev0, ev1;
@@ -1559,10 +1566,11 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       c->launches += 2;
       Fuse = Fd;
     }
+    shift_now = shift * std::min(1.0, err_prev / kShiftFade);
     if (shift != 0.0) {  // F + b (S - 1/2 S D S)
       gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, S, Dm, T1);
       gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, S, T2);
-      cku(k_level_shift(Fuse, S, T2, shift, (long long)nn, Fsh, s));
+      cku(k_level_shift(Fuse, S, T2, shift_now, (long long)nn, Fsh, s));
       c->launches++;
       Fuse = Fsh;
     }
@@ -1581,6 +1589,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     double err;
     std::memcpy(&err, &bits, 8);
     const double e_cur = hs[0], e_ref = hs[1];
+    err_prev = err;
     bool done;
     if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) done = err < c->opt.epsilon;
     else done = iter > 0 && std::fabs(e_cur - e_prev) < c->opt.epsilon && err < std::sqrt(c->opt.epsilon);
@@ -1622,7 +1631,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
           for (int k = 0; k < n; ++k)
             res->coefficient_matrix[(size_t)i * n + k] = hC[(size_t)k * n + i] * (flip ? c->fsign[i] : 1.0);
       if (res->orbital_energies)  // the level shift lifted the virtual orbitals by b
-        for (int k = 0; k < n; ++k) res->orbital_energies[k] = evals[k] - (k >= nocc ? shift : 0.0);
+        for (int k = 0; k < n; ++k) res->orbital_energies[k] = evals[k] - (k >= nocc ? shift_now : 0.0);
       result = FOCK_OK;
       break;
     }
@@ -1800,6 +1809,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   double *Fring = (double*)mk(TB * ring), *Ering = (double*)mk(TB * ring);
   const double shift = c->opt.level_shift;
   double* Fsh = shift != 0.0 ? (double*)mk(TB) : F;
+  double* d_bmol = (double*)mk((size_t)nmol * 8);  // level shift of every molecule this iteration
   double* Bm = (double*)mk((size_t)nmol * ring * ring * 8);
   double* coef = (double*)mk((size_t)nmol * (ring + 1) * 8);
   double* ecur = (double*)mk((size_t)nmol * 8);
@@ -1903,7 +1913,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   const bool refine = mixed && c->opt.final_fp64;
   std::vector<unsigned char> mode(nmol, mixed ? 1 : 2);
   std::vector<int> done(nmol, 0), ready(nmol, 0);
-  std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol);
+  std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol, 1.0), bmol(nmol, 0.0);
   std::vector<unsigned long long> hb(nmol);
   for (int k = 0; k < nmol; ++k) {
     fock_scf_result& o = results[b->perm[k]];
@@ -2002,10 +2012,12 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       Fuse = Fd;
     }
     phase(1, tp);
-    if (shift != 0.0) {  // F + b (S - 1/2 S D S), every block
+    if (shift != 0.0) {  // F + b_m (S - 1/2 S D S), every block, b_m fading with molecule m's error
+      for (int k = 0; k < nmol; ++k) bmol[k] = shift * std::min(1.0, errv[k] / kShiftFade);
+      cku(cudaMemcpyAsync(d_bmol, bmol.data(), nmol * 8, cudaMemcpyHostToDevice, s));
       for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, S, Dm, T1);
       for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, S, T2);
-      cku(k_level_shift(Fuse, S, T2, shift, T, Fsh, s));
+      cku(kb_level_shift(Fuse, S, T2, d_bmol, c->d_mol_off, nmol, T, Fsh, s));
       c->launches++;
       Fuse = Fsh;
     }

@@ -198,6 +198,25 @@ cudaError_t k_add(const double* a, const double* b, double* c, int nn, cudaStrea
   add_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, c, nn);
   return cudaGetLastError();
 }
+// Level shift with one b per molecule block (batched layout: block m starts at off[m]).
+__global__ void level_shift_blocks_kernel(const double* F, const double* S, const double* SDS,
+                                          const double* __restrict__ b, const long long* __restrict__ off, int nmol,
+                                          long long total, double* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  int lo = 0, hi = nmol - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= t) lo = mid; else hi = mid - 1;
+  }
+  const double bm = b[lo];
+  out[t] = F[t] + bm * S[t] - 0.5 * bm * SDS[t];
+}
+cudaError_t kb_level_shift(const double* F, const double* S, const double* SDS, const double* b, const long long* off,
+                           int nmol, long long total, double* out, cudaStream_t s) {
+  level_shift_blocks_kernel<<<blocks_for(total, 256), 256, 0, s>>>(F, S, SDS, b, off, nmol, total, out);
+  return cudaGetLastError();
+}
 cudaError_t k_level_shift(const double* F, const double* S, const double* SDS, double b, long long nn, double* out,
                           cudaStream_t s) {
   level_shift_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(F, S, SDS, b, nn, out);

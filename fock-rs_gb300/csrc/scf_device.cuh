@@ -7,6 +7,9 @@ cudaError_t k_add(const double* a, const double* b, double* c, int nn, cudaStrea
 // out = F + b S - (b/2) SDS (level shift of the virtual space), nn elements
 cudaError_t k_level_shift(const double* F, const double* S, const double* SDS, double b, long long nn, double* out,
                           cudaStream_t s);
+// the same per molecule block with shift b[m] (batched layout, block offsets off)
+cudaError_t kb_level_shift(const double* F, const double* S, const double* SDS, const double* b, const long long* off,
+                           int nmol, long long total, double* out, cudaStream_t s);
 cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s);
 cudaError_t k_symmetrize_blocks(const double* M, double* G, const long long* off, const int* n, int nmol,
                                 long long total, cudaStream_t s);

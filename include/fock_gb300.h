@@ -100,9 +100,12 @@ typedef struct {
   int shard_count;          /* launch with r % shard_count == shard_index (G is then a partial sum;
                                summing the partial G of all shards, e.g. by an all-reduce, gives G) */
   double level_shift;       /* SCF level shift b (Eh): the matrix diagonalised each iteration is
-                               F + b (S - 1/2 S D S), which lifts the virtual orbitals by b and damps
-                               occupied-virtual mixing.  Self-consistent solutions are unchanged;
-                               reported orbital energies are unshifted.  0 = the reference's loop. */
+                               F + b' (S - 1/2 S D S), which lifts the virtual orbitals by b' and damps
+                               occupied-virtual mixing; b' = b while the previous max|FDS - SDF| is
+                               >= 0.1 and b times that error / 0.1 below it (per molecule in
+                               batches), so the last iterations are plain DIIS.  Self-consistent
+                               solutions are unchanged; reported orbital energies are unshifted.
+                               0 = the reference's loop. */
 } fock_options;
 
 typedef struct {
