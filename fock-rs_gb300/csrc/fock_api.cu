@@ -36,7 +36,10 @@ using namespace fockgb;
 namespace {
 
 constexpr int kMaxL = 2;
-constexpr int kForkStreams = 8;
+#ifndef FOCK_FORK_STREAMS
+#define FOCK_FORK_STREAMS 32
+#endif
+constexpr int kForkStreams = FOCK_FORK_STREAMS;
 // mixed-precision SCF: switch to FP64 Fock builds once max|FDS - SDF| < this
 constexpr double kMixedSwitch = 1e-4;
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
