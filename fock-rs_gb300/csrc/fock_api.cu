@@ -42,6 +42,11 @@ constexpr int kMaxL = 2;
 constexpr int kForkStreams = FOCK_FORK_STREAMS;
 // mixed-precision SCF: switch to FP64 Fock builds once max|FDS - SDF| < this
 constexpr double kMixedSwitch = 1e-4;
+// ... or once the mixed-phase error has stopped halving for kMixedStall
+// iterations below kMixedStallErr (the FP32 noise floor of a large molecule
+// can sit above kMixedSwitch), or after half of max_iters.
+constexpr int kMixedStall = 3;
+constexpr double kMixedStallErr = 1e-2;
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
 
 inline int pair_class(int la, int lb) { return la * (la + 1) / 2 + lb; }
@@ -1532,6 +1537,8 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   int next_slot = 0;
   double e_prev = 0.0;
   double err_prev = 1.0, shift_now = 0.0;  // previous DIIS error; shift of this iteration
+  double err_best = 1e300;                  // mixed phase: smallest error so far and
+  int stall = 0;                            // iterations since it last halved
   double fock_ms = 0.0;
   int builds = 0;
   cudaEvent_t ev0, ev1;
@@ -1596,8 +1603,10 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     bool done;
     if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) done = err < c->opt.epsilon;
     else done = iter > 0 && std::fabs(e_cur - e_prev) < c->opt.epsilon && err < std::sqrt(c->opt.epsilon);
-    if (mixed && c->opt.final_fp64 && !refc && !fp64_phase && (done || err < kMixedSwitch) &&
-        iter < c->opt.max_iters) {
+    if (err < 0.5 * err_best) { err_best = err; stall = 0; } else { ++stall; }
+    const bool floor = stall >= kMixedStall && err < kMixedStallErr;
+    if (mixed && c->opt.final_fp64 && !refc && !fp64_phase &&
+        (done || err < kMixedSwitch || floor || iter >= c->opt.max_iters / 2) && iter < c->opt.max_iters) {
       // mixed phase close to convergence: the remaining iterations (and the
       // reported energy) are FP64, so the result carries no FP32 error
       int r = fock_set_precision(c, FOCK_PREC_FP64, c->opt.mixed_threshold);
@@ -1916,7 +1925,8 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   const bool refine = mixed && c->opt.final_fp64;
   std::vector<unsigned char> mode(nmol, mixed ? 1 : 2);
   std::vector<int> done(nmol, 0), ready(nmol, 0);
-  std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol, 1.0), bmol(nmol, 0.0);
+  std::vector<double> he(nmol), hr(nmol), eprev(nmol, 0.0), errv(nmol, 1.0), bmol(nmol, 0.0), err_best(nmol, 1e300);
+  std::vector<int> stall(nmol, 0);
   std::vector<unsigned long long> hb(nmol);
   for (int k = 0; k < nmol; ++k) {
     fock_scf_result& o = results[b->perm[k]];
@@ -2053,7 +2063,9 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
         else conv = iter > 0 && std::fabs(he[k] - eprev[k]) < c->opt.epsilon && errv[k] < std::sqrt(c->opt.epsilon);
         if (mode[k] == 1 && refine && !last) {
           // mixed phase: close to convergence (or half the iterations gone) -> FP64 at the next re-plan
-          if (conv || errv[k] < kMixedSwitch || iter >= c->opt.max_iters / 2) ready[k] = 1;
+          if (errv[k] < 0.5 * err_best[k]) { err_best[k] = errv[k]; stall[k] = 0; } else { ++stall[k]; }
+          const bool floor = stall[k] >= kMixedStall && errv[k] < kMixedStallErr;
+          if (conv || errv[k] < kMixedSwitch || floor || iter >= c->opt.max_iters / 2) ready[k] = 1;
         } else if (conv || last) {
           finish(k, iter, conv);
         }
