@@ -108,6 +108,9 @@ def lib():
         L.fock_strerror.argtypes = [C.c_int]
         L.fock_strerror.restype = C.c_char_p
         L.fock_measure_fma_peak.argtypes = [C.c_int, C.c_int, dp]
+        L.fock_read_xyz.argtypes = [C.c_char_p, C.POINTER(Atom), C.c_int, ip]
+        L.fock_basis_shells.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Atom), C.c_int, C.POINTER(Shell), C.c_int,
+                                        dp, dp, C.c_int, ip, ip]
         fp = C.POINTER(C.c_float)
         L.fock_orbital_grid.argtypes = [vp, dp, C.c_int, C.c_double, C.c_double, fp]
         L.fock_orbital_grid_device.argtypes = [vp, dp, C.c_int, C.c_double, C.c_double, vp]

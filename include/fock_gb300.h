@@ -214,6 +214,28 @@ int fock_orbital_grid(fock_ctx* ctx, const double* coef, int nvox, double box, d
 int fock_orbital_grid_device(fock_ctx* ctx, const double* coef, int nvox, double box, double min_coef,
                              float* grid_dev);
 
+/* Readers of the formats on either side of the path (host only, no GPU needed).
+ *
+ * fock_read_xyz: chemfiles/src/xyz.rs:13-32 -- every match of the reference's
+ * pattern "symbol x y z" (Angstrom) in the file becomes an atom, coordinates
+ * scaled by the reference's factor 1.89 to bohr; elements H..Kr by symbol
+ * (an unknown symbol is FOCK_ERR_INVALID_ARG, where the reference panics).
+ * Writes at most `capacity` atoms; *natom = atoms found (FOCK_ERR_TOO_LARGE
+ * when they do not fit).
+ *
+ * fock_basis_shells: basis_set/src/lib.rs:79-118 -- the shells of every atom, in
+ * atom order, from a MolSSI BSE JSON file ({"elements": {"Z": {"electron_shells":
+ * [...]}}}) or, with `name`, from the entry `name` of a collection of such sets
+ * (the set itself or a bare {"Z": [shells]} map).  Entries with several angular
+ * momenta (SP) give one shell per angular momentum, in order; coefficients are
+ * the raw contraction coefficients (fock_ctx_create normalises).  exps/coefs:
+ * caller buffers of prim_capacity doubles that the shells point into; *nshell
+ * and *nprim = the counts needed (FOCK_ERR_TOO_LARGE when they do not fit). */
+int fock_read_xyz(const char* path, fock_atom* atoms, int capacity, int* natom);
+int fock_basis_shells(const char* json_path, const char* name, const fock_atom* atoms, int natom,
+                      fock_shell* shells, int shell_capacity, double* exps, double* coefs, int prim_capacity,
+                      int* nshell, int* nprim);
+
 /* Use an external CUDA stream (cudaStream_t) for all work of this context;
  * NULL restores the context's own stream. */
 int fock_set_stream(fock_ctx* ctx, void* stream);
