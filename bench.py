@@ -467,13 +467,8 @@ def main():
     from fock_gb300 import _lib
     cap = 512
 
-    class Prof(C.Structure):
-        _fields_ = [("la", C.c_int), ("lb", C.c_int), ("lc", C.c_int), ("ld", C.c_int), ("prec", C.c_int),
-                    ("quartets", C.c_longlong), ("prim_quartets", C.c_longlong), ("flops", C.c_longlong),
-                    ("ms", C.c_float)]
-    arr = (Prof * cap)()
+    arr = (_lib.LaunchProfile * cap)()
     lib = _lib.lib()
-    lib.fock_profile_build.argtypes = [C.c_void_p, C.c_void_p, C.POINTER(Prof), C.c_int]
     per_class = {}
     for _ in range(3):
         flush.fill_(1.0)

@@ -60,6 +60,19 @@ class Stats(C.Structure):
                 ("flops_fp64", C.c_longlong), ("flops_fp32", C.c_longlong), ("launches_per_build", C.c_int)]
 
 
+class LaunchProfile(C.Structure):
+    """fock_launch_profile: one class launch of a profiled build."""
+    _fields_ = [("la", C.c_int), ("lb", C.c_int), ("lc", C.c_int), ("ld", C.c_int), ("prec", C.c_int),
+                ("quartets", C.c_longlong), ("prim_quartets", C.c_longlong), ("flops", C.c_longlong),
+                ("ms", C.c_float)]
+
+
+class Tuning(C.Structure):
+    """fock_tuning: launch parameters chosen by the autotuner."""
+    _fields_ = [("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int), ("block_threads", C.c_int),
+                ("persistent", C.c_int), ("ms", C.c_float)]
+
+
 _lib = None
 
 
@@ -108,6 +121,10 @@ def lib():
         L.fock_strerror.argtypes = [C.c_int]
         L.fock_strerror.restype = C.c_char_p
         L.fock_measure_fma_peak.argtypes = [C.c_int, C.c_int, dp]
+        L.fock_profile_build.argtypes = [vp, vp, C.POINTER(LaunchProfile), C.c_int]
+        L.fock_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
+        L.fock_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
+        L.fock_batch_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
         L.fock_read_xyz.argtypes = [C.c_char_p, C.POINTER(Atom), C.c_int, ip]
         L.fock_basis_shells.argtypes = [C.c_char_p, C.c_char_p, C.POINTER(Atom), C.c_int, C.POINTER(Shell), C.c_int,
                                         dp, dp, C.c_int, ip, ip]

@@ -11,23 +11,11 @@ import json
 import os
 
 from . import _lib
-from ._lib import check, lib
-
-
-class Tuning(C.Structure):
-    _fields_ = [("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int), ("block_threads", C.c_int),
-                ("persistent", C.c_int), ("ms", C.c_float)]
+from ._lib import Tuning, check, lib
 
 
 def _declare():
-    L = lib()
-    if not getattr(L, "_tuning_declared", False):
-        vp = C.c_void_p
-        L.fock_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
-        L.fock_set_tuning.argtypes = [vp, C.POINTER(Tuning)]
-        L.fock_batch_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
-        L._tuning_declared = True
-    return L
+    return lib()
 
 
 def default_cache_path():

@@ -26,6 +26,13 @@ def test_library_exports_every_header_symbol(gpu_lib):
         assert hasattr(gpu_lib, name), name
 
 
+def test_python_mirror_declares_every_header_function(gpu_lib):
+    """Every C entry point has its ctypes signature in fock_gb300._lib (no call
+    goes through ctypes' default int conversions)."""
+    missing = [n for n in header_functions() if getattr(getattr(gpu_lib, n), "argtypes", None) is None]
+    assert not missing, missing
+
+
 def test_options_defaults_match_reference_constants(gpu_lib):
     from fock_gb300 import options
     o = options()
