@@ -39,6 +39,7 @@ import numpy as np  # noqa: E402
 METRIC = "ERI+Fock quartets/s (C6H6 RHF/6-31G Fock build)"
 UNIT = "quartets/s"
 BATCH_LEVEL_SHIFT = 1.0  # Eh; SCF level shift of the batched water-cluster workload
+BUILD_DRAM_BYTES_NCU = 25.0e6  # bytes per benzene FP64 build under ncu (launch list, 4 builds / 4)
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
             "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
 
@@ -503,7 +504,13 @@ def main():
                 "kernel": "eri_kernel class launches of one FP64 Fock build (one CUDA graph, %d launches)"
                           % st["launches_per_build"],
                 "achieved": build_achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": build_achieved / peak if peak else None, "traffic": None,
+                "frac": build_achieved / peak if peak else None,
+                # DRAM bytes of the six class kernels of one build, read from the ncu launch list of
+                # `bench.py --only benzene` (cold caches, serialised launches); the warm concurrent
+                # build reads its pair data and tables from L2
+                "traffic": BUILD_DRAM_BYTES_NCU,
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one build's class "
+                                  "launches (profiles/fock_build_benzene_631g_launch_list.md)",
                 "flops_per_build": build_flops,
                 "peak_source": "measured FP64 FMA microbenchmark in this run (fock_measure_fma_peak); "
                                "MEASURED_PEAKS.json has no FP64 figure",
