@@ -134,3 +134,25 @@ def test_reference_arm_prints_contract_line(oracle_lib):
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+
+
+def test_header_is_plain_c_and_links(gpu_lib, tmp_path):
+    """include/fock_gb300.h compiles as strict C99 and a C program links against the library
+    (what a cgo / bindgen / plain-C caller sees); options come back with the defaults."""
+    import shutil
+    import subprocess
+    from fock_gb300 import _lib as L
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    src = tmp_path / "t.c"
+    src.write_text('#include "fock_gb300.h"\n#include <stdio.h>\n'
+                   'int main(void) { fock_options o; fock_options_default(&o);\n'
+                   '  printf("%d %d %d\\n", o.diis_len, o.diis_start, o.shard_count); return 0; }\n')
+    libdir = os.path.dirname(L.LIB_PATH)
+    exe = tmp_path / "t"
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lfock_gb300",
+                        "-Wl,-rpath," + libdir, "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0 and out.stdout.split() == ["16", "5", "1"]
