@@ -238,9 +238,10 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
     return out
 
 
-def benzene_builds(torch, F, L, local, flush, steps=3, warmup=3):
-    """FP64 Fock builds of the headline workload alone (no SCF): for launch lists and captures."""
-    ctx = F.FockContext(benzene_atoms(), sign_convention=L.FOCK_SIGN_STANDARD, device=local)
+def benzene_builds(torch, F, L, local, flush, steps=3, warmup=3, precision=None):
+    """Fock builds of the headline workload alone (no SCF): for launch lists and captures."""
+    precision = L.FOCK_PREC_FP64 if precision is None else precision
+    ctx = F.FockContext(benzene_atoms(), sign_convention=L.FOCK_SIGN_STANDARD, device=local, precision=precision)
     n = ctx.n
     rng = np.random.default_rng(0)
     Cm = rng.normal(size=(n, 21)) / np.sqrt(n)
@@ -255,7 +256,7 @@ def benzene_builds(torch, F, L, local, flush, steps=3, warmup=3):
             "flops_fp64": st["flops_fp64"]}
 
 
-def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
+def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=False):
     """(H2O)_32 cluster (seed 0), RHF/6-31G* with Cartesian d on O: 608 functions.
     FP64 and mixed Fock builds at a density of 160 random orthonormal-ish orbitals."""
     from fock_gb300 import basis as B, molecules as M
@@ -282,6 +283,8 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3):
     out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_build"] / out["mixed"]["ms_per_build"]
     out["mixed"]["single_build_energy_error_eh"] = abs(0.5 * float((D * (Gs["mixed"] - Gs["fp64"])).sum().item()))
     ctx.close()
+    if builds_only:
+        return out
     # mixed-precision SCF (final iterations FP64) and the nuclear gradient: analytic
     # derivative kernels for the s/p classes, finite-difference kernels for the d classes
     with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
@@ -376,7 +379,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scf", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batch, (H2O)32 and gradient workloads")
-    ap.add_argument("--only", choices=["benzene", "batch", "water32", "octane"],
+    ap.add_argument("--only", choices=["benzene", "benzene_mixed", "batch", "water32", "water32_builds", "octane"],
                     help="run one side workload alone (profiling) and print its JSON")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -396,6 +399,9 @@ def main():
     if args.only:
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         fn = {"benzene": lambda: benzene_builds(torch, F, L, local, flush, args.steps, args.warmup),
+              "benzene_mixed": lambda: benzene_builds(torch, F, L, local, flush, args.steps, args.warmup,
+                                                      L.FOCK_PREC_MIXED),
+              "water32_builds": lambda: water32_workload(torch, F, L, local, flush, args.steps, args.warmup, True),
               "batch": lambda: batch_workload(torch, F, L, local, flush, args.steps, args.warmup),
               "water32": lambda: water32_workload(torch, F, L, local, flush, args.steps, args.warmup),
               "octane": lambda: octane_gradient_workload(torch, F, L, local)}[args.only]

@@ -36,7 +36,7 @@ def _deps_mtime():
     for root in (CSRC, GEN, os.path.join(os.path.dirname(HERE), "include")):
         for f in os.listdir(root):
             p = os.path.join(root, f)
-            if os.path.isfile(p) and f.endswith((".cu", ".cuh", ".h", ".py")):
+            if os.path.isfile(p) and f.endswith((".cu", ".cuh", ".h", ".py", ".inc")):
                 m = max(m, os.path.getmtime(p))
     return m
 
@@ -58,12 +58,29 @@ def _compile(src, verbose):
     return obj
 
 
+def write_ref_lut():
+    """gen/ref_lut.inc: the reference's stored Boys table (data/boys_ref_lut.json)
+    as a C array for the reference-compatible mode."""
+    import json
+    with open(os.path.join(HERE, "data", "boys_ref_lut.json")) as f:
+        vals = json.load(f)["values"]
+    assert len(vals) == 200
+    body = ",\n".join("  %r" % float(v) for v in vals)
+    text = ("// Generated by build.py from data/boys_ref_lut.json. Do not edit.\n"
+            "static const double kRefBoysLut[200] = {\n%s};\n" % body)
+    path = os.path.join(GEN, "ref_lut.inc")
+    if not os.path.exists(path) or open(path).read() != text:
+        with open(path, "w") as f:
+            f.write(text)
+
+
 def build(verbose=False, jobs=None):
     sys.path.insert(0, CSRC)
     import gen_eri  # noqa
     sys.path.pop(0)
     os.makedirs(GEN, exist_ok=True)
     gen_eri.main(GEN, LMAX)
+    write_ref_lut()
     os.makedirs(OBJ, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = _sources()

@@ -25,7 +25,10 @@ constexpr int kBoysMaxM = 12;           // orders with a Taylor table
 constexpr double kBoysTmax = 64.0;
 constexpr float kBoysTmaxF = 64.0f;
 
-enum Mode { MODE_JK = 0, MODE_TENSOR = 1, MODE_SCHWARZ = 2, MODE_GRAD = 3 };
+// MODE_PRELOAD launches nothing: it queries the attributes of the class's
+// Fock-build kernels, which makes the runtime load their code (lazy module
+// loading) ahead of calls that must not allocate device memory.
+enum Mode { MODE_JK = 0, MODE_TENSOR = 1, MODE_SCHWARZ = 2, MODE_GRAD = 3, MODE_PRELOAD = 4 };
 enum Prec { PREC_FP64 = 0, PREC_FP32 = 1 };
 
 // Contracted shell pair (a, b), la >= lb (equal l: shell a >= shell b).

@@ -439,6 +439,16 @@ enum LaunchPart { PART_JK64 = 0, PART_JK32 = 1, PART_PERSISTENT = 2, PART_AUX = 
 
 template <class C, int PART>
 cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if (mode == MODE_PRELOAD) {
+    cudaFuncAttributes fa;
+    if constexpr (PART == PART_JK64) return cudaFuncGetAttributes(&fa, eri_kernel<C, double, MODE_JK>);
+    if constexpr (PART == PART_JK32) return cudaFuncGetAttributes(&fa, eri_kernel<C, float, MODE_JK>);
+    if constexpr (PART == PART_PERSISTENT) {
+      cudaError_t e = cudaFuncGetAttributes(&fa, eri_kernel_persistent<C, double>);
+      return e == cudaSuccess ? cudaFuncGetAttributes(&fa, eri_kernel_persistent<C, float>) : e;
+    }
+    return cudaSuccess;
+  }
   if constexpr (PART == PART_AUX) {
     if (mode == MODE_GRAD) {
       if constexpr (C::HAS_GRAD) {
@@ -496,6 +506,12 @@ cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int p
 
 template <class C>
 cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int prec, cudaStream_t s) {
+  if (mode == MODE_PRELOAD) {
+    cudaError_t e = launch_part<C, PART_JK64>(cl, a, mode, prec, s);
+    if (e == cudaSuccess) e = launch_part<C, PART_JK32>(cl, a, mode, prec, s);
+    if (e == cudaSuccess) e = launch_part<C, PART_PERSISTENT>(cl, a, mode, prec, s);
+    return e;
+  }
   if (mode == MODE_GRAD || mode == MODE_SCHWARZ || mode == MODE_TENSOR)
     return launch_part<C, PART_AUX>(cl, a, mode, prec, s);
   if (cl.queue && cl.persist_blocks != 0) return launch_part<C, PART_PERSISTENT>(cl, a, mode, prec, s);

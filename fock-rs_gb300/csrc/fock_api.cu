@@ -59,6 +59,7 @@ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 // (positive terms, no cancellation) for the top order in long double, then
 // the stable downward recursion F_{n-1} = (2T F_n + e^{-T}) / (2n-1).
 // ---------------------------------------------------------------------------
+#include "gen/ref_lut.inc"
 constexpr int kTabOrders = kBoysMaxM + kBoysTaylor;  // F_0 .. F_{M+6}
 std::once_flag g_tab_once;
 std::vector<double> g_boys64, g_ref_lut;
@@ -103,9 +104,8 @@ void build_tables() {
       g_boys64[row + kBoysTaylor] = (double)ex;
       g_boys32[row + kBoysTaylor] = (float)ex;
     }
-  // reference LUT: F_10(0.15 k), k < 200 (boys/src/lut.rs values, regenerated)
-  g_ref_lut.resize(200);
-  for (int k = 0; k < 200; ++k) g_ref_lut[k] = (double)boys_series_ld(10, (long double)((double)k * 0.15));
+  // reference LUT: F_10(0.15 k), k < 200, the values stored in boys/src/lut.rs
+  g_ref_lut.assign(kRefBoysLut, kRefBoysLut + 200);
 }
 
 // reference normalisation of a Cartesian primitive (basis/src/primitives.rs:19-27)
@@ -626,6 +626,7 @@ int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri) {
 
 int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int nshell, const fock_options* opt,
                const int* mol_shell_begin, int nmol, fock_ctx** out);
+int fockgb_noalloc_setup(fock_ctx* c);  // noalloc.cu
 
 extern "C" {
 
@@ -952,6 +953,7 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   }
   if ((rc = compute_schwarz(c)) != FOCK_OK) return fail(rc);
   if ((rc = build_plan(c, false)) != FOCK_OK) return fail(rc);
+  if (nmol == 1 && (rc = fockgb_noalloc_setup(c)) != FOCK_OK) return fail(rc);
   *out = c;
   return FOCK_OK;
 }
@@ -973,6 +975,14 @@ int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
 // first, so that the small classes fill in behind them: a single small
 // molecule has too few quartets per class to fill 152 SMs on its own), join,
 // G = M + M^T.  Captured once per plan, replayed per build.
+// Class launches of a build, largest first (by model flops).
+static std::vector<int> plan_order(const fock_ctx* c) {
+  std::vector<int> order(c->plans.size());
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return c->plans[x].flops > c->plans[y].flops; });
+  return order;
+}
+
 static int capture_jk_graph(fock_ctx* c) {
   if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
   const size_t nn = (size_t)c->total_elems;
@@ -980,9 +990,7 @@ static int capture_jk_graph(fock_ctx* c) {
   EriArgs a = eri_args(c);
   bool need32 = false;
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
-  std::vector<int> order(c->plans.size());
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return c->plans[x].flops > c->plans[y].flops; });
+  const std::vector<int> order = plan_order(c);
   const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
   CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
@@ -1032,11 +1040,18 @@ int fock_build_jk_device(fock_ctx* c, const double* D_dev, double* G_dev) {
 }  // extern "C"
 
 // Fock build with caller-provided working memory (accumulator M and the FP32
-// density copy), used by the allocation-free entry point in noalloc.cu.
+// density copy), used by the allocation-free entry point in noalloc.cu.  The
+// same launches as the captured build, issued directly: clear M, re-arm the
+// work queues of persistent launches, FP32 copy of D, the class launches
+// forked over the context's side streams (largest first), join, G = M + M^T.
+// Nothing here allocates: memsets, event records and waits, kernel launches.
 int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, double* M, float* D32) {
   const int n = c->nbf;
   const size_t nn = (size_t)n * n;
-  CK(cudaMemsetAsync(M, 0, nn * sizeof(double), c->stream));
+  cudaStream_t cs = c->stream;
+  CK(cudaMemsetAsync(M, 0, nn * sizeof(double), cs));
+  if (c->opt.persistent)
+    CK(cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, (c->plans.size() + 1) * sizeof(long long), cs));
   EriArgs a = eri_args(c);
   a.D = D_dev;
   a.D32 = D32;
@@ -1044,16 +1059,45 @@ int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, dou
   bool need32 = false;
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
   if (need32) {
-    CK(k_to_float(D_dev, D32, (int)nn, c->stream));
+    CK(k_to_float(D_dev, D32, (int)nn, cs));
     c->launches++;
   }
-  for (const Plan& p : c->plans) {
-    cudaError_t e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->stream);
+  const std::vector<int> order = plan_order(c);
+  const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
+  cudaError_t e = cudaEventRecord(c->fork_ev, cs);
+  int forked = 0;
+  for (; forked < nside && e == cudaSuccess; ++forked) e = cudaStreamWaitEvent(c->side[forked], c->fork_ev, 0);
+  for (size_t k = 0; k < order.size() && e == cudaSuccess; ++k) {
+    const Plan& p = c->plans[order[k]];
+    e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->side[k % nside]);
     c->launches++;
-    CK(e);
   }
-  CK(k_symmetrize(M, G_dev, n, c->stream));
+  // join every side stream that took part, also after an error
+  for (int s = 0; s < forked; ++s) {
+    cudaError_t e2 = cudaEventRecord(c->join_ev[s], c->side[s]);
+    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(cs, c->join_ev[s], 0);
+    if (e == cudaSuccess) e = e2;
+  }
+  CK(e);
+  CK(k_symmetrize(M, G_dev, n, cs));
   c->launches++;
+  return FOCK_OK;
+}
+
+// Loads the code of every kernel a Fock build of this context can launch
+// (every class of its catalog, FP64, FP32 and persistent forms, and the
+// helper kernels), so that builds never load modules lazily.
+int fockgb_preload_build(fock_ctx* c) {
+  std::vector<int> seen;
+  EriArgs a = eri_args(c);
+  ClassLaunch cl{};
+  for (const CatGroup& G : c->catalog.groups) {
+    const int key = ((G.la * 8 + G.lb) * 8 + G.lc) * 8 + G.ld;
+    if (std::find(seen.begin(), seen.end(), key) != seen.end()) continue;
+    seen.push_back(key);
+    CK(launch_eri_class(G.la, G.lb, G.lc, G.ld, cl, a, MODE_PRELOAD, PREC_FP64, c->stream));
+  }
+  CK(k_preload_build_kernels());
   return FOCK_OK;
 }
 
@@ -1397,6 +1441,37 @@ int fock_energy_backward(fock_ctx* c, const fock_scf_result* r, double* grad) {
       W[(size_t)i * n + j] = 2.0 * s;
     }
   return fock_gradient(c, r->density_matrix, W.data(), grad);
+}
+
+int fock_boys_eval(int device, int form, int order, const double* T, int n, double* out) {
+  if (!T || !out || n < 0 || form < FOCK_BOYS_FP64 || form > FOCK_BOYS_MD || order < 0 ||
+      order > (form == FOCK_BOYS_REFERENCE ? 10 : kBoysMaxM))
+    return FOCK_ERR_INVALID_ARG;
+  for (int i = 0; i < n; ++i)
+    if (!(T[i] >= 0.0) || !std::isfinite(T[i])) return FOCK_ERR_INVALID_ARG;
+  if (n == 0) return FOCK_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return FOCK_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(device));
+  std::call_once(g_tab_once, build_tables);
+  double *d_tab = nullptr, *d_lut = nullptr, *d_T = nullptr, *d_out = nullptr;
+  float* d_tab32 = nullptr;
+  const size_t nout = (size_t)n * (order + 1);
+  cudaError_t e = dalloc(&d_tab, g_boys64.size());
+  if (e == cudaSuccess) e = dalloc(&d_tab32, g_boys32.size());
+  if (e == cudaSuccess) e = dalloc(&d_lut, g_ref_lut.size());
+  if (e == cudaSuccess) e = dalloc(&d_T, (size_t)n);
+  if (e == cudaSuccess) e = dalloc(&d_out, nout);
+  if (e == cudaSuccess) e = cudaMemcpy(d_tab, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_tab32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(d_T, T, (size_t)n * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = md_boys_eval(form, order, d_T, n, d_tab, d_tab32, d_lut, d_out, 0);
+  if (e == cudaSuccess) e = cudaMemcpy(out, d_out, nout * 8, cudaMemcpyDeviceToHost);
+  dfree(d_tab); dfree(d_tab32); dfree(d_lut); dfree(d_T); dfree(d_out);
+  CK(e);
+  return FOCK_OK;
 }
 
 int fock_measure_fma_peak(int device, int fp64, double* gflops) {

@@ -527,4 +527,66 @@ cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* 
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// The device Boys functions at caller-given arguments (accuracy tests of the
+// exact code the kernels run): form 0 = boys_scaled<L> in FP64 (ERI kernels),
+// 1 = boys_scaled<L> in FP32 (mixed-precision ERI kernels), 2 = the reference
+// LUT function boys_ref_dev, 3 = boys_exact_all (MD kernels).  One thread per
+// argument writes F_0..F_L to out[i * (L + 1) ...].
+// ---------------------------------------------------------------------------
+namespace {
+template <int L>
+__global__ void boys_eval_kernel(int form, const double* __restrict__ T, int n, const double* __restrict__ tab64,
+                                 const float* __restrict__ tab32, const double* __restrict__ lut, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double t = T[i];
+  double* o = out + (size_t)i * (L + 1);
+  if (form == 0) {
+    double F[L + 1];
+    boys_scaled<L>(t, 1.0, tab64, F);
+    for (int m = 0; m <= L; ++m) o[m] = F[m];
+  } else if (form == 1) {
+    float F[L + 1];
+    boys_scaled<L>((float)t, 1.0f, tab32, F);
+    for (int m = 0; m <= L; ++m) o[m] = (double)F[m];
+  } else if (form == 2) {
+    for (int m = 0; m <= L; ++m) o[m] = boys_ref_dev(t, m, lut);
+  } else {
+    double F[kBoysMaxM + 1];
+    boys_exact_all(t, L, tab64, F);
+    for (int m = 0; m <= L; ++m) o[m] = F[m];
+  }
+}
+
+template <int L>
+cudaError_t boys_eval_launch(int form, const double* T, int n, const double* tab64, const float* tab32,
+                             const double* lut, double* out, cudaStream_t s) {
+  boys_eval_kernel<L><<<(n + 127) / 128, 128, 0, s>>>(form, T, n, tab64, tab32, lut, out);
+  return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t md_boys_eval(int form, int order, const double* T, int n, const double* tab64, const float* tab32,
+                         const double* lut, double* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  switch (order) {
+    case 0: return boys_eval_launch<0>(form, T, n, tab64, tab32, lut, out, s);
+    case 1: return boys_eval_launch<1>(form, T, n, tab64, tab32, lut, out, s);
+    case 2: return boys_eval_launch<2>(form, T, n, tab64, tab32, lut, out, s);
+    case 3: return boys_eval_launch<3>(form, T, n, tab64, tab32, lut, out, s);
+    case 4: return boys_eval_launch<4>(form, T, n, tab64, tab32, lut, out, s);
+    case 5: return boys_eval_launch<5>(form, T, n, tab64, tab32, lut, out, s);
+    case 6: return boys_eval_launch<6>(form, T, n, tab64, tab32, lut, out, s);
+    case 7: return boys_eval_launch<7>(form, T, n, tab64, tab32, lut, out, s);
+    case 8: return boys_eval_launch<8>(form, T, n, tab64, tab32, lut, out, s);
+    case 9: return boys_eval_launch<9>(form, T, n, tab64, tab32, lut, out, s);
+    case 10: return boys_eval_launch<10>(form, T, n, tab64, tab32, lut, out, s);
+    case 11: return boys_eval_launch<11>(form, T, n, tab64, tab32, lut, out, s);
+    case 12: return boys_eval_launch<12>(form, T, n, tab64, tab32, lut, out, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 }  // namespace fockgb

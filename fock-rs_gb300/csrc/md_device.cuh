@@ -41,4 +41,10 @@ cudaError_t md_g_from_tensor(const double* eri, const double* D, int n, double* 
 cudaError_t md_orbital_grid(const MdBasis& B, const int* sel, const double* csel, int nsel, int nvox, double box,
                             float* out, cudaStream_t s);
 
+// F_0..F_order at n arguments (device arrays) by one of the device Boys forms
+// (0: FP64 Taylor table of the ERI kernels, 1: its FP32 form, 2: the reference
+// LUT function, 3: the MD kernels' runtime-order form); order <= 12.
+cudaError_t md_boys_eval(int form, int order, const double* T, int n, const double* tab64, const float* tab32,
+                         const double* lut, double* out, cudaStream_t s);
+
 }  // namespace fockgb

@@ -17,9 +17,10 @@
 //   * every call on a device uses the same arrays: calls whose work overlaps
 //     on the GPU (other streams, other contexts, other host threads) race and
 //     corrupt each other's results.  Serialise them.
-//   * the first call on a device looks up the arrays' device addresses
-//     (cudaGetSymbolAddress, with that device current); make that first call
-//     before any stream capture on the device.
+//   * the set-up is done by fock_ctx_create, with the context's device
+//     current: it looks up the arrays' device addresses (cudaGetSymbolAddress,
+//     once per device) and loads the code of every kernel the context's builds
+//     launch, so that neither happens lazily inside a call.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -28,6 +29,7 @@
 
 int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, double* M, float* D32);
 int fockgb_ctx_device(const fock_ctx* c);
+int fockgb_preload_build(fock_ctx* c);
 
 namespace {
 
@@ -49,18 +51,15 @@ DeviceScratch g_scratch[kMaxDevices];
 
 }  // namespace
 
-extern "C" int fock_build_jk_noalloc(fock_ctx* ctx, const double* D_dev, double* G_dev) {
-  if (!ctx || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
-  const int n = fock_nbasis(ctx);
-  if (n > kMaxBasis) return FOCK_ERR_TOO_LARGE;
-  const int dev = fockgb_ctx_device(ctx);
-  if (dev < 0 || dev >= kMaxDevices) return FOCK_ERR_INVALID_ARG;
-  if (cudaSetDevice(dev) != cudaSuccess) return FOCK_ERR_CUDA;
-  DeviceScratch s;
+// Set-up for one context, called by context creation with the context's
+// device current.  Contexts too large for the entry point need none.
+int fockgb_noalloc_setup(fock_ctx* c) {
+  if (fock_nbasis(c) > kMaxBasis) return FOCK_OK;
+  const int dev = fockgb_ctx_device(c);
+  if (dev < 0 || dev >= kMaxDevices) return FOCK_OK;  // the entry point rejects such contexts
   {
     std::lock_guard<std::mutex> lock(g_mu);
     if (!g_scratch[dev].M) {
-      // one-time set-up on this device (the device is current)
       double* m = nullptr;
       float* f = nullptr;
       if (cudaGetSymbolAddress((void**)&m, g_noalloc_M) != cudaSuccess) return FOCK_ERR_CUDA;
@@ -68,7 +67,27 @@ extern "C" int fock_build_jk_noalloc(fock_ctx* ctx, const double* D_dev, double*
       g_scratch[dev].M = m;
       g_scratch[dev].D32 = f;
     }
+  }
+  return fockgb_preload_build(c);
+}
+
+extern "C" int fock_build_jk_noalloc(fock_ctx* ctx, const double* D_dev, double* G_dev) {
+  if (!ctx || !D_dev || !G_dev) return FOCK_ERR_INVALID_ARG;
+  const int n = fock_nbasis(ctx);
+  if (n > kMaxBasis) return FOCK_ERR_TOO_LARGE;
+  const int dev = fockgb_ctx_device(ctx);
+  if (dev < 0 || dev >= kMaxDevices) return FOCK_ERR_INVALID_ARG;
+  DeviceScratch s;
+  {
+    std::lock_guard<std::mutex> lock(g_mu);
     s = g_scratch[dev];
   }
-  return fockgb_build_jk_scratch(ctx, D_dev, G_dev, s.M, s.D32);
+  if (!s.M || !s.D32) return FOCK_ERR_CUDA;  // set-up at context creation did not run
+  // the calling thread's current device is left as it was
+  int prev = -1;
+  if (cudaGetDevice(&prev) != cudaSuccess) return FOCK_ERR_CUDA;
+  if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return FOCK_ERR_CUDA;
+  const int rc = fockgb_build_jk_scratch(ctx, D_dev, G_dev, s.M, s.D32);
+  if (prev != dev) cudaSetDevice(prev);
+  return rc;
 }

@@ -235,6 +235,12 @@ cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s) {
   to_float_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, nn);
   return cudaGetLastError();
 }
+// Loads the code of the helper kernels of a Fock build (see MODE_PRELOAD).
+cudaError_t k_preload_build_kernels() {
+  cudaFuncAttributes fa;
+  cudaError_t e = cudaFuncGetAttributes(&fa, symmetrize_kernel);
+  return e == cudaSuccess ? cudaFuncGetAttributes(&fa, to_float_kernel) : e;
+}
 cudaError_t k_guess(const double* S, const double* H, double* F, int n, int gwh, cudaStream_t s) {
   guess_kernel<<<blocks_for((long long)n * n, 256), 256, 0, s>>>(S, H, F, n, gwh);
   return cudaGetLastError();

@@ -15,7 +15,9 @@ FOCK_PREC_FP64, FOCK_PREC_MIXED = 0, 1
 FOCK_ERI_EXACT, FOCK_ERI_REFCOMPAT = 0, 1
 FOCK_GUESS_GWH, FOCK_GUESS_CORE = 0, 1
 FOCK_CONV_COMMUTATOR, FOCK_CONV_ENERGY = 0, 1
-FOCK_ERR_DIVERGED = -5
+FOCK_BOYS_FP64, FOCK_BOYS_FP32, FOCK_BOYS_REFERENCE, FOCK_BOYS_MD = 0, 1, 2, 3
+FOCK_ERR_INVALID_ARG, FOCK_ERR_UNSUPPORTED_L, FOCK_ERR_OOM = -1, -2, -3
+FOCK_ERR_DIVERGED, FOCK_ERR_CUDA, FOCK_ERR_TOO_LARGE = -5, -7, -8
 
 EXPORTED = [
     "fock_options_default", "fock_ctx_create", "fock_ctx_destroy", "fock_nbasis", "fock_set_precision",
@@ -121,6 +123,7 @@ def lib():
         L.fock_strerror.argtypes = [C.c_int]
         L.fock_strerror.restype = C.c_char_p
         L.fock_measure_fma_peak.argtypes = [C.c_int, C.c_int, dp]
+        L.fock_boys_eval.argtypes = [C.c_int, C.c_int, C.c_int, dp, C.c_int, dp]
         L.fock_profile_build.argtypes = [vp, vp, C.POINTER(LaunchProfile), C.c_int]
         L.fock_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
         L.fock_set_tuning.argtypes = [vp, C.POINTER(Tuning)]

@@ -164,10 +164,15 @@ int fock_build_jk_device(fock_ctx* ctx, const double* D_dev, double* G_dev);
  * library's device image.  That array is held by every GPU that loads the
  * library, until the process exits.
  *   - n_basis <= FOCK_NOALLOC_MAX_BASIS, else FOCK_ERR_TOO_LARGE;
- *   - the first call on a device looks up the array's device address; make
- *     that first call before any stream capture on that device;
- *   - all calls on a device share the array: calls whose GPU work overlaps
- *     (other streams, contexts or threads) race and corrupt each other.
+ *   - the set-up is part of fock_ctx_create (which allocates anyway): with
+ *     the context's device current it looks up the array's device address
+ *     (once per device) and loads the code of every kernel the context's
+ *     builds can launch, so no call loads a module lazily;
+ *   - the calling thread's current device is left unchanged;
+ *   - all calls on a device share the array, which keeps the last call's
+ *     contents (each call clears what must start at zero): calls whose GPU
+ *     work overlaps (other streams, contexts or threads) race and corrupt
+ *     each other.
  * Inputs and outputs as fock_build_jk_device (device pointers, textbook sign
  * convention, queued on the context's stream). */
 #define FOCK_NOALLOC_MAX_BASIS 256
@@ -311,6 +316,23 @@ int fock_set_tuning(fock_ctx* ctx, const fock_tuning* t);
 int fock_batch_autotune(fock_batch* batch, const double* D_dev, int reps, fock_tuning* best);
 
 const char* fock_strerror(int code);
+
+/* The device Boys functions F_0(t)..F_order(t) at n host arguments t >= 0,
+ * out[i * (order + 1) + m] = F_m(T[i]), evaluated on the device by the same
+ * code the kernels run (accuracy tests; no counterpart in the reference, whose
+ * boys(t, n) is boys/src/lib.rs:58-81):
+ *   FOCK_BOYS_FP64       Taylor table + downward recursion of the FP64 ERI kernels
+ *   FOCK_BOYS_FP32       the FP32 form of the mixed-precision ERI kernels
+ *   FOCK_BOYS_REFERENCE  the reference's function (F_10 LUT of boys/src/lut.rs,
+ *                        linear interpolation, index clamp, asymptotic t >= 30),
+ *                        as used by FOCK_ERI_REFCOMPAT; order <= 10
+ *   FOCK_BOYS_MD         the runtime-order form of the one-electron kernels
+ * order <= 12 otherwise. */
+#define FOCK_BOYS_FP64 0
+#define FOCK_BOYS_FP32 1
+#define FOCK_BOYS_REFERENCE 2
+#define FOCK_BOYS_MD 3
+int fock_boys_eval(int device, int form, int order, const double* T, int n, double* out);
 
 /* FP64 / FP32 FMA-pipe throughput microbenchmark on this device: fills
  * *gflops with the measured rate (2 flops per FMA). */

@@ -125,6 +125,8 @@ constexpr int kLutN = 200;  // (MAX_TABULATED_T / DT) as usize
 double g_lut[kLutN];
 bool g_lut_ready = false;
 
+// The table is the reference's stored one (boys/src/lut.rs), handed over by
+// orc_set_lut; without it, the exact F_10 at the same nodes stands in.
 void init_lut() {
   if (g_lut_ready) return;
   for (int k = 0; k < kLutN; ++k) g_lut[k] = boys_exact((double)k * kDT, kMaxN);
@@ -670,6 +672,12 @@ double orc_boys(double t, int n, int flags) {
 double orc_boys_lut_entry(int k) {
   init_lut();
   return (k >= 0 && k < kLutN) ? g_lut[k] : NAN;
+}
+
+// Installs the reference's stored table (200 values of F_10(0.15 k)).
+void orc_set_lut(const double* values) {
+  for (int k = 0; k < kLutN; ++k) g_lut[k] = values[k];
+  g_lut_ready = true;
 }
 
 double orc_hermite_expansion(int i, int j, int t, double dist, double a, double b) {

@@ -58,6 +58,17 @@ class ScfResult(C.Structure):
 
 
 _lib = None
+LUT_PATH = os.path.join(os.path.dirname(HERE), "fock-rs_gb300", "data", "boys_ref_lut.json")
+
+
+def reference_lut():
+    """F_10(0.15 k), k < 200, as stored in the reference's boys/src/lut.rs."""
+    import json
+    with open(LUT_PATH) as f:
+        vals = json.load(f)["values"]
+    assert len(vals) == 200
+    return vals
+
 
 
 def lib():
@@ -93,6 +104,10 @@ def lib():
         L.orc_ref_build_timed.argtypes = [C.POINTER(_Basis), dp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                           dp, dp]
         L.orc_max_threads.restype = C.c_int
+        L.orc_set_lut.argtypes = [dp]
+        # the reference's stored Boys table (data file shared with the library)
+        lut = np.ascontiguousarray(reference_lut(), dtype=np.float64)
+        L.orc_set_lut(_dp(lut))
         _lib = L
     return _lib
 

@@ -1,9 +1,13 @@
 """Generate the committed golden fixtures under tests/golden/.
 
-Run once in a checkout that has the reference sources (default path
-/root/reference) and mpmath:  python tests/golden/make_golden.py [ref_root]
+Run once where the reference sources and mpmath are present:
+  FOCK_REFERENCE_ROOT=<fock-rs checkout> python tests/golden/make_golden.py [--lut-only]
 
 Fixtures
+  fock-rs_gb300/data/boys_ref_lut.json
+                       the reference's 200 stored F_10 values (boys/src/lut.rs),
+                       read by the library's reference-compatible mode and by
+                       the oracle (--lut-only writes this file alone).
   boys_mpmath.json     F_n(t) at 30 digits (mpmath), n = 0..12, t on a log grid
                        plus points next to the Boys table nodes.
   h2o_sto3g_ref.json   H2O / STO-3G (the water workload), computed by a pure-
@@ -269,10 +273,25 @@ def scf_reference(S, H, eri4, nel, max_iters=100, eps=1e-6):
     return None
 
 
-def make_h2o(ref_root):
+def read_lut(ref_root):
+    """The reference's stored F_10(0.15 k), k < 200 (boys/src/lut.rs), as written there."""
     src = open(os.path.join(ref_root, "boys/src/lut.rs")).read()
     lut = [float(x) for x in re.findall(r"[-+0-9.eE]+(?=,)", src.split("=", 1)[1])]
     assert len(lut) == 200
+    return lut
+
+
+def write_lut(ref_root):
+    """Data file shared by the library's reference-compatible mode and the oracle."""
+    dst = os.path.join(os.path.dirname(os.path.dirname(HERE)), "fock-rs_gb300", "data", "boys_ref_lut.json")
+    with open(dst, "w") as f:
+        json.dump({"source": "boys/src/lut.rs of fock-rs (F_10(0.15 k), k = 0..199, as stored there)",
+                   "dt": 0.15, "order": 10, "values": read_lut(ref_root)}, f, indent=0)
+    print("wrote", dst)
+
+
+def make_h2o(ref_root):
+    lut = read_lut(ref_root)
     Zs, xyz = M.water_sto3g()
     atoms = B.build_atoms("STO-3G", Zs, xyz)
     fs = functions(atoms)
@@ -309,7 +328,10 @@ def make_h2o(ref_root):
     return out
 
 
-def main(ref_root):
+def main(ref_root, lut_only=False):
+    write_lut(ref_root)
+    if lut_only:
+        return
     with open(os.path.join(HERE, "boys_mpmath.json"), "w") as f:
         json.dump(make_boys(), f)
     with open(os.path.join(HERE, "h2o_sto3g_ref.json"), "w") as f:
@@ -317,4 +339,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = os.environ.get("FOCK_REFERENCE_ROOT")
+    if not root:
+        sys.exit("set FOCK_REFERENCE_ROOT to the root of a fock-rs checkout")
+    main(root, lut_only="--lut-only" in sys.argv[1:])

@@ -11,7 +11,8 @@ from fock_gb300 import molecules as M
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 DATA = os.path.join(ROOT, "fock-rs_gb300", "data", "basis_sets.json")
-REF_DATA = "/root/reference/basis_set/src/data"
+# root of a fock-rs checkout, for the comparison with its BSE files (skipped without it)
+REF_DATA = os.path.join(os.environ.get("FOCK_REFERENCE_ROOT", "/nonexistent"), "basis_set", "src", "data")
 
 
 def test_read_xyz_matches_python_reader(gpu_lib, tmp_path):

@@ -10,7 +10,8 @@ import pytest
 from fock_gb300 import basis as B
 from fock_gb300 import molecules as M
 
-REF = "/root/reference"
+# root of a fock-rs checkout, for the tests that read its sources (skipped without it)
+REF = os.environ.get("FOCK_REFERENCE_ROOT", "")
 
 
 def test_hermite_expansion_doctest_golden(oracle_lib):
@@ -30,17 +31,25 @@ def test_boys_exact_vs_mpmath(oracle_lib, golden_boys):
     assert worst < 5e-14, worst
 
 
-def test_boys_reference_lut_matches_reference_file(oracle_lib):
+def test_boys_reference_lut_is_the_stored_table(oracle_lib):
+    # the oracle's LUT is the data file of the reference's stored values, bit for bit
+    stored = oracle_lib.reference_lut()
+    ours = [oracle_lib.lib().orc_boys_lut_entry(k) for k in range(200)]
+    assert ours == stored
+    # the reference's table came from a quadrature crate: within 1e-11 of the exact F_10
+    exact = [oracle_lib.boys(0.15 * k, 10, oracle_lib.EXACT) for k in range(200)]
+    rel = max(abs(a - b) / abs(b) for a, b in zip(stored, exact))
+    assert rel < 1e-11, rel
+
+
+def test_boys_lut_data_file_matches_reference_file(oracle_lib):
     path = os.path.join(REF, "boys/src/lut.rs")
-    if not os.path.exists(path):
-        pytest.skip("reference sources not present")
+    if not REF or not os.path.exists(path):
+        pytest.skip("FOCK_REFERENCE_ROOT (reference sources) not set")
     import re
     src = open(path).read()
     lut = [float(x) for x in re.findall(r"[-+0-9.eE]+(?=,)", src.split("=", 1)[1])]
-    ours = [oracle_lib.lib().orc_boys_lut_entry(k) for k in range(200)]
-    rel = max(abs(a - b) / abs(b) for a, b in zip(ours, lut))
-    # the reference's table came from a quadrature crate; ours is the exact F_10
-    assert rel < 1e-11, rel
+    assert oracle_lib.reference_lut() == lut
 
 
 def test_boys_reference_behaviour(oracle_lib):
