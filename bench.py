@@ -39,6 +39,7 @@ import numpy as np  # noqa: E402
 METRIC = "ERI+Fock quartets/s (C6H6 RHF/6-31G Fock build)"
 UNIT = "quartets/s"
 BATCH_LEVEL_SHIFT = 1.0  # Eh; SCF level shift of the batched water-cluster workload
+MIXED_CURVE = (1.0, 0.1, 0.01, 1e-3, 1e-4)  # mixed thresholds of the batch's speed / accuracy curve
 BUILD_DRAM_BYTES_NCU = 25.0e6  # bytes per benzene FP64 build under ncu (launch list, 4 builds / 4)
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
             "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
@@ -224,6 +225,23 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
     dG = Gs["mixed"] - Gs["fp64"]
     de = [0.5 * float((D[o:o + n * n] * dG[o:o + n * n]).sum().item()) for o, n in zip(b.offsets, b.nbf)]
     res_prec["mixed"]["max_single_build_energy_error_eh"] = max(abs(x) for x in de)
+    # speed / accuracy curve of one mixed build over the threshold (density-weighted split)
+    curve = []
+    for th in MIXED_CURVE:
+        b.set_precision(L.FOCK_PREC_MIXED, th)
+        t = _event_times(torch, stream, lambda: b.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
+        ms_c = sum(t) / len(t)
+        dGc = G - Gs["fp64"]
+        dec = [0.5 * float((D[o:o + n * n] * dGc[o:o + n * n]).sum().item()) for o, n in zip(b.offsets, b.nbf)]
+        stc = b.stats()
+        curve.append({"mixed_threshold": th, "ms_per_build": ms_c,
+                      "speedup_vs_fp64": res_prec["fp64"]["ms_per_build"] / ms_c,
+                      "max_single_build_energy_error_eh": max(abs(x) for x in dec),
+                      "fp32_shell_quartets": stc["shell_quartets_fp32"], "fp64_shell_quartets": stc["shell_quartets_fp64"]})
+    res_prec["mixed_threshold_curve"] = curve
+    ok = [c for c in curve if c["max_single_build_energy_error_eh"] <= 1e-6]
+    res_prec["best_speedup_at_1e-6_eh_per_build"] = max((c["speedup_vs_fp64"] for c in ok), default=None)
+    b.set_precision(L.FOCK_PREC_MIXED, F.options().mixed_threshold)
     out.update(res_prec)
     # spot check: molecules solved alone in FP64 against the batched mixed SCF
     idx = np.linspace(0, len(mols) - 1, spot).astype(int)
@@ -234,6 +252,18 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
             worst = max(worst, abs(r.total_energy - res[i].total_energy))
     out["scf_mixed"]["max_abs_energy_error_vs_single_fp64_eh"] = worst
     out["scf_mixed"]["spot_checked_molecules"] = [int(i) for i in idx]
+    # the same batched SCF in plain FP64, for the SCF-time ratio of the metric
+    b.set_precision(L.FOCK_PREC_FP64, F.options().mixed_threshold)
+    t0 = time.perf_counter()
+    rc64, res64, _ = b.scf(densities=True)
+    torch.cuda.synchronize()
+    wall64 = time.perf_counter() - t0
+    out["scf_fp64"] = {"rc": rc64, "wall_s": wall64, "fock_s": res64[0].fock_seconds,
+                       "fock_builds": res64[0].fock_builds, "converged": sum(r.converged for r in res64),
+                       "iterations_max": max(r.iterations for r in res64)}
+    out["scf_mixed"]["speedup_vs_fp64_scf"] = wall64 / out["scf_mixed"]["wall_s"]
+    out["scf_mixed"]["max_abs_energy_error_vs_batched_fp64_eh"] = max(
+        abs(a.total_energy - r.total_energy) for a, r in zip(res, res64) if a.converged and r.converged)
     b.close()
     return out
 
@@ -300,6 +330,17 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
     out["scf_mixed"] = {"rc": rc, "wall_s": scf_s, "iterations": r.iterations, "energy": r.total_energy,
                         "level_shift_eh": BATCH_LEVEL_SHIFT, "energy_per_water": r.total_energy / 32,
                         "converged": bool(r.converged), "fock_builds": r.fock_builds, "fock_s": r.fock_seconds}
+    with F.FockContext(atoms, precision=L.FOCK_PREC_FP64, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
+                       energy_mode=1, epsilon=1e-8, max_iters=100, level_shift=BATCH_LEVEL_SHIFT,
+                       device=local) as fctx:
+        t0 = time.perf_counter()
+        rc64, r64, _, _, _ = fctx.scf(0)
+        torch.cuda.synchronize()
+        scf64_s = time.perf_counter() - t0
+    out["scf_fp64"] = {"rc": rc64, "wall_s": scf64_s, "iterations": r64.iterations, "energy": r64.total_energy,
+                       "converged": bool(r64.converged), "fock_builds": r64.fock_builds, "fock_s": r64.fock_seconds}
+    out["scf_mixed"]["speedup_vs_fp64_scf"] = scf64_s / scf_s
+    out["scf_mixed"]["abs_energy_error_vs_fp64_eh"] = abs(r.total_energy - r64.total_energy)
     out["gradient"] = {"wall_s": grad_s, "max_abs": float(np.abs(g).max()),
                        "net_force": float(np.abs(g.sum(axis=0)).max()), "components": int(g.size)}
     return out
@@ -515,8 +556,9 @@ def main():
                 # `bench.py --only benzene` (cold caches, serialised launches); the warm concurrent
                 # build reads its pair data and tables from L2
                 "traffic": BUILD_DRAM_BYTES_NCU,
-                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over one build's class "
-                                  "launches (profiles/fock_build_benzene_631g_launch_list.md)",
+                "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum summed over one build's class "
+                                  "launches, from the launch list of `bench.py --only benzene` (cold caches, "
+                                  "serialised launches), not measured in this run",
                 "flops_per_build": build_flops,
                 "peak_source": "measured FP64 FMA microbenchmark in this run (fock_measure_fma_peak); "
                                "MEASURED_PEAKS.json has no FP64 figure",
@@ -549,6 +591,15 @@ def main():
              "single_build_energy_error_eh": abs(de_build)}
     if rmx is not None:
         mixed["abs_energy_error_vs_fp64_eh"] = abs(rmx.total_energy - r64.total_energy)
+    # error per ERI of the FP32 kernels: the benzene tensor with every quartet in FP32
+    t64 = F.ElectronTensor.from_basis(atoms, device=local).data
+    t32 = F.ElectronTensor.from_basis(atoms, device=local, precision=L.FOCK_PREC_MIXED, mixed_threshold=1e30).data
+    err = np.abs(t32 - t64)
+    big = np.abs(t64) > 1e-3
+    mixed["fp32_eri_error"] = {"max_abs": float(err.max()), "rms_abs": float(np.sqrt((err ** 2).mean())),
+                               "max_rel_for_abs_above_1e-3": float((err[big] / np.abs(t64[big])).max()),
+                               "integrals": int(t64.size)}
+    del t64, t32, err
 
     # ---- e2e through the C ABI with host buffers ----
     Dh = np.ascontiguousarray(r64.density_matrix)

@@ -88,6 +88,7 @@ pub struct fock_options {
     pub shard_index: c_int,
     pub shard_count: c_int,
     pub level_shift: c_double,
+    pub mixed_density: c_int,
 }
 
 #[repr(C)]
@@ -205,6 +206,8 @@ extern "C" {
     pub fn fock_batch_autotune(batch: *mut fock_batch, D_dev: *const c_double, reps: c_int,
                                best: *mut fock_tuning) -> c_int;
     pub fn fock_strerror(code: c_int) -> *const c_char;
+    pub fn fock_sorted_eigs(device: c_int, n: c_int, A: *const c_double, evals: *mut c_double,
+                            evecs: *mut c_double) -> c_int;
     pub fn fock_boys_eval(device: c_int, form: c_int, order: c_int, T: *const c_double, n: c_int,
                           out: *mut c_double) -> c_int;
     pub fn fock_measure_fma_peak(device: c_int, fp64: c_int, gflops: *mut c_double) -> c_int;

@@ -25,7 +25,7 @@ def nvcc():
 
 
 def _sources():
-    srcs = [os.path.join(CSRC, f) for f in ("fock_api.cu", "md_device.cu", "scf_device.cu", "noalloc.cu",
+    srcs = [os.path.join(CSRC, f) for f in ("fock_api.cu", "md_device.cu", "scf_device.cu", "noalloc.cu", "eigen.cu",
                                             "loaders.cpp")]
     srcs += sorted(os.path.join(GEN, f) for f in os.listdir(GEN) if f.startswith("inst_") and f.endswith(".cu"))
     return srcs

@@ -40,6 +40,7 @@ struct PairInfo {
   float Q;        // Schwarz factor sqrt(max |(ab|ab)|)
   int cls;        // pair class index
   double AB[3];   // A - B
+  float ABf[3];   // A - B rounded to float (FP32 lanes)
   int atom_a, atom_b;  // centres of shells a and b (gradient)
   int mol_off;    // offset of this molecule's n x n block in D, M, G (batches)
   int mol_n;      // basis size of this molecule: row stride of that block
@@ -92,6 +93,15 @@ struct ClassLaunch {
   int block;                     // threads per block (0: default)
   int persist_blocks;            // > 0: persistent launch with this many blocks
   unsigned long long* queue;     // work-queue counter of the persistent launch
+  // Density-weighted precision split of a mixed build: a lane whose ket index
+  // within its row is below row_split[r] tests the quartet's bound
+  // Q_ab Q_cd max|D| (max over the six density blocks it is contracted with,
+  // float arithmetic identical in both precisions) against wthr; FP64
+  // launches keep the quartets at or above wthr, FP32 launches the others, so
+  // the two launches of a class partition their common rows.  nullptr: no test.
+  const int* row_split;
+  float wthr;
+  unsigned long long* counters;  // [0] quartets, [1] primitive quartets computed (nullptr: not counted)
 };
 
 struct EriArgs {
@@ -124,6 +134,17 @@ __device__ __forceinline__ float approx_float(double x) {
   const int e = ((hi >> 20) & 0x7ff) - 1023 + 127;
   const int bits = (e << 23) | ((hi & 0xfffff) << 3);
   return e <= 0 ? 0.0f : (e >= 255 ? __int_as_float(0x7f800000) : __int_as_float(bits));
+}
+
+// float -> double with integer operations only (exact for normal floats;
+// zeros and subnormals give a signed zero), so that FP32 lanes spend no
+// FP64-pipe conversion on the values they hand to FP64 atomics.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  const unsigned hi = (u & 0x80000000u) | (e ? (((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)) : 0u);
+  const unsigned lo = e ? (u << 29) : 0u;
+  return __hiloint2double((int)hi, (int)lo);
 }
 
 // 1/sqrt(x) in double: single-precision hardware estimate refined by one

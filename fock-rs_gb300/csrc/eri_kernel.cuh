@@ -24,8 +24,8 @@ namespace fockgb {
 constexpr int kEriThreads = 128;     // default block size (tunable per launch: 64..256)
 constexpr int kEriMaxThreads = 256;
 
-// unroll factor of the ket primitive loop (independent iterations interleave:
-// instruction-level parallelism for the long FP64 dependency chains)
+// unroll factor of the inner (bra) primitive loop (independent iterations
+// interleave: instruction-level parallelism for the long FP64 dependency chains)
 #ifndef FOCK_KET_UNROLL
 #define FOCK_KET_UNROLL 2
 #endif
@@ -102,9 +102,21 @@ __device__ __forceinline__ float dens<float>(const EriArgs& a, size_t mo, int ld
   return __ldg(a.D32 + mo + (size_t)i * ld + j);
 }
 
+// A - B of a pair in the lane's precision (the float copy for FP32 lanes).
+template <typename R>
+__device__ __forceinline__ R pair_ab(const PairInfo& P, int i);
+template <>
+__device__ __forceinline__ double pair_ab<double>(const PairInfo& P, int i) { return P.AB[i]; }
+template <>
+__device__ __forceinline__ float pair_ab<float>(const PairInfo& P, int i) { return P.ABf[i]; }
+
+__device__ __forceinline__ double to_f64(double x) { return x; }
+__device__ __forceinline__ double to_f64(float x) { return f2d_exact(x); }
+
 // Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
+// Also returns the row (*row) and the ket's index within it (*kloc).
 __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, int& bra, int& ket, int& slice,
-                                            int& nslice) {
+                                            int& nslice, int* row = nullptr, int* kloc = nullptr) {
   int lo = 0, hi = cl.nrows - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -117,6 +129,27 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
   const int k = (int)(local - (long long)slice * cnt);
   bra = __ldg(cl.bra_list + lo);
   ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
+  if (row) *row = lo;
+  if (kloc) *kloc = k;
+}
+
+// max |D| over the six density blocks a quartet is contracted with (ab, cd,
+// ac, ad, bc, bd), from the float density copy: the same value in the FP64
+// and the FP32 launches of a class.
+template <class C>
+__device__ __forceinline__ float quartet_dmax(const EriArgs& a, size_t mo, int ld, int fa, int fb, int fc, int fd) {
+  float w = 0.0f;
+  auto blk = [&](int f0, int n0, int f1, int n1) {
+    for (int i = 0; i < n0; ++i)
+      for (int j = 0; j < n1; ++j) w = fmaxf(w, fabsf(__ldg(a.D32 + mo + (size_t)(f0 + i) * ld + f1 + j)));
+  };
+  blk(fa, C::NA, fb, C::NB);
+  blk(fc, C::NC, fd, C::ND);
+  blk(fa, C::NA, fc, C::NC);
+  blk(fa, C::NA, fd, C::ND);
+  blk(fb, C::NB, fc, C::NC);
+  blk(fb, C::NB, fd, C::ND);
+  return w;
 }
 
 // The work of lane t of a launch (one contracted quartet, one bra slice).
@@ -131,7 +164,16 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
     bra = ket = cl.bra_list[active ? t : 0];
   } else {
     if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
-    decode_lane(cl, t, bra, ket, slice, nslice);
+    int row, kloc;
+    decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc);
+    if (MODE == MODE_JK && cl.row_split && kloc < __ldg(cl.row_split + row)) {
+      // density-weighted precision split: this launch keeps its side of the bound
+      const PairInfo& Pb = a.pairs[bra];
+      const PairInfo& Pk = a.pairs[ket];
+      const float w = quartet_dmax<C>(a, (size_t)Pb.mol_off, Pb.mol_n, Pb.fa, Pb.fb, Pk.fa, Pk.fb);
+      const bool heavy = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), w) >= cl.wthr;
+      if (heavy != (sizeof(R) == sizeof(double))) return;
+    }
     active = true;
   }
   const PairInfo& Pb = a.pairs[bra];
@@ -141,19 +183,33 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   const int ib1 = (int)(((long long)(slice + 1) * Pb.nprim) / nslice);
   const int nkp = active ? Pk.nprim : 0;
   const int bp0 = Pb.prim_off, kp0 = Pk.prim_off;
+  if (MODE == MODE_JK && cl.counters) {
+    // work actually computed (the split is decided per build): one atomic per warp
+    const unsigned m = __activemask();
+    const unsigned pq = __reduce_add_sync(m, (unsigned)((ib1 - ib0) * nkp));
+    const unsigned q = __reduce_add_sync(m, slice == 0 ? 1u : 0u);
+    if ((threadIdx.x & 31) == __ffs(m) - 1) {
+      atomicAdd(cl.counters, (unsigned long long)q);
+      atomicAdd(cl.counters + 1, (unsigned long long)pq);
+    }
+  }
 
   R acc[NE * NF];
 #pragma unroll
   for (int i = 0; i < NE * NF; ++i) acc[i] = R(0);
 
   const R* btab = boys_table<R>(a);
-  for (int ib = ib0; ib < ib1; ++ib) {
-    PrimLoad<R> bp;
-    bp.load(a, bp0 + ib);
+  // ket primitive pairs outer, bra primitive pairs inner: a lane's ket records
+  // (scattered: every lane of a warp has its own ket) are read once per slice,
+  // while the bra records of the inner loop are the same for all lanes of a
+  // row and load as broadcasts
+  for (int ik = 0; ik < nkp; ++ik) {
+    PrimLoad<R> kp;
+    kp.load(a, kp0 + ik);
 #pragma unroll kKetUnroll
-    for (int ik = 0; ik < nkp; ++ik) {
-      PrimLoad<R> kp;
-      kp.load(a, kp0 + ik);
+    for (int ib = ib0; ib < ib1; ++ib) {
+      PrimLoad<R> bp;
+      bp.load(a, bp0 + ib);
       R rs, o2pq, rp, rq, rho;  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho from the exponent-sum table
       bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
@@ -170,7 +226,7 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
 
   R AB[3], CD[3];
 #pragma unroll
-  for (int i = 0; i < 3; ++i) { AB[i] = (R)Pb.AB[i]; CD[i] = (R)Pk.AB[i]; }
+  for (int i = 0; i < 3; ++i) { AB[i] = pair_ab<R>(Pb, i); CD[i] = pair_ab<R>(Pk, i); }
   R out[NA * NB * NC * ND];
   C::template hrr<R>(acc, AB, CD, out);
   if (C::LA >= 2 || C::LB >= 2 || C::LC >= 2 || C::LD >= 2) {
@@ -279,28 +335,30 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
             kbc[ib * NC + ic] += v * Dad[ia * ND + id];
           }
   }
-  const double sdeg = (Pb.sa == Pb.sb ? 0.5 : 1.0) * (Pk.sa == Pk.sb ? 0.5 : 1.0) * (bra == ket ? 0.5 : 1.0);
-  const double sj = 2.0 * sdeg, sk = -0.5 * sdeg;
+  // degeneracy factors are powers of two: exact in either precision, so the
+  // scaling runs in the lane's own precision (FP32 lanes issue no FP64-pipe op)
+  const R sdeg = (Pb.sa == Pb.sb ? R(0.5) : R(1)) * (Pk.sa == Pk.sb ? R(0.5) : R(1)) * (bra == ket ? R(0.5) : R(1));
+  const R sj = R(2) * sdeg, sk = R(-0.5) * sdeg;
   if (!active) return;
 #pragma unroll
-  for (int i = 0; i < NA * NB; ++i) atomicAdd(a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB), sj * (double)jab[i]);
+  for (int i = 0; i < NA * NB; ++i) atomicAdd(a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB), to_f64(sj * jab[i]));
 #pragma unroll
   for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fc + ic) * ld + (fd + id), sj * (double)jcd[ic * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fc + ic) * ld + (fd + id), to_f64(sj * jcd[ic * ND + id]));
 #pragma unroll
   for (int ia = 0; ia < NA; ++ia) {
 #pragma unroll
-    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fc + ic), sk * (double)kac[ia * NC + ic]);
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fc + ic), to_f64(sk * kac[ia * NC + ic]));
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fd + id), sk * (double)kad[ia * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fa + ia) * ld + (fd + id), to_f64(sk * kad[ia * ND + id]));
   }
 #pragma unroll
   for (int ib = 0; ib < NB; ++ib) {
 #pragma unroll
-    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fc + ic), sk * (double)kbc[ib * NC + ic]);
+    for (int ic = 0; ic < NC; ++ic) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fc + ic), to_f64(sk * kbc[ib * NC + ic]));
 #pragma unroll
-    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fd + id), sk * (double)kbd[ib * ND + id]);
+    for (int id = 0; id < ND; ++id) atomicAdd(a.M + mo + (size_t)(fb + ib) * ld + (fd + id), to_f64(sk * kbd[ib * ND + id]));
   }
 }
 
@@ -478,6 +536,9 @@ cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int p
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   if constexpr (PART == PART_AUX) {
     eri_kernel<C, double, MODE_TENSOR><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
+  } else if constexpr (PART == PART_JK32) {
+    if (mode == MODE_TENSOR) eri_kernel<C, float, MODE_TENSOR><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
+    else eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   } else if constexpr (PART == PART_PERSISTENT) {
     // persistent: half of the resident capacity of the GPU (other classes run
     // beside it on the other streams of the captured build)
@@ -496,8 +557,6 @@ cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int p
     if (pb > blocks) pb = blocks;
     if (prec == PREC_FP32) eri_kernel_persistent<C, float><<<(unsigned)pb, thr, 0, s>>>(cl, a);
     else eri_kernel_persistent<C, double><<<(unsigned)pb, thr, 0, s>>>(cl, a);
-  } else if constexpr (PART == PART_JK32) {
-    eri_kernel<C, float, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   } else {
     eri_kernel<C, double, MODE_JK><<<(unsigned)blocks, thr, 0, s>>>(cl, a);
   }
@@ -512,6 +571,7 @@ cudaError_t launch_class(const ClassLaunch& cl, const EriArgs& a, int mode, int 
     if (e == cudaSuccess) e = launch_part<C, PART_PERSISTENT>(cl, a, mode, prec, s);
     return e;
   }
+  if (mode == MODE_TENSOR && prec == PREC_FP32) return launch_part<C, PART_JK32>(cl, a, mode, prec, s);
   if (mode == MODE_GRAD || mode == MODE_SCHWARZ || mode == MODE_TENSOR)
     return launch_part<C, PART_AUX>(cl, a, mode, prec, s);
   if (cl.queue && cl.persist_blocks != 0) return launch_part<C, PART_PERSISTENT>(cl, a, mode, prec, s);

@@ -28,6 +28,7 @@
 #include "../../include/fock_gb300.h"
 #include "common.cuh"
 #include "gen/dispatch.cuh"
+#include "eigen.cuh"
 #include "md_device.cuh"
 #include "scf_device.cuh"
 
@@ -46,6 +47,13 @@ constexpr double kMixedSwitch = 1e-4;
 // iterations below kMixedStallErr (the FP32 noise floor of a large molecule
 // can sit above kMixedSwitch), or after half of max_iters.
 constexpr int kMixedStall = 3;
+// mixed precision: classes with la + lb + lc + ld above this (Boys orders 7 and
+// 8: (dd|dp), (dd|dd)) are never split to FP32
+constexpr int kMixedMaxL = 6;
+// density-weighted split: largest max|D| the plan's FP64 candidates allow for
+// (quartets of larger density blocks run in FP32 unless their Schwarz product
+// alone reaches mixed_threshold / kDensityPlanMax)
+constexpr double kDensityPlanMax = 2.0;
 constexpr double kMixedStallErr = 1e-2;
 constexpr int kNumPairClasses = (kMaxL + 1) * (kMaxL + 2) / 2;
 
@@ -127,6 +135,7 @@ struct Plan {
   int la, lb, lc, ld, prec;
   ClassLaunch cl;
   long long quartets, prim_quartets, flops;
+  long long flops_pq, flops_q;  // model flops per primitive quartet and per contracted quartet
 };
 
 int map_cuda(cudaError_t e) {
@@ -213,7 +222,9 @@ struct fock_ctx {
   // plans
   std::vector<Plan> plans;
   int* d_plan_int = nullptr;
-  size_t queue_base = 0;  // first work-queue counter in d_plan_ll
+  size_t queue_base = 0;  // first work-queue counter in d_plan_ll (plans + 1), then the
+                          // work counters of a density-weighted mixed plan (2 per plan)
+  bool split_counts = false;  // the plans carry row_split and counters
   long long* d_plan_ll = nullptr;
   fock_stats stats{};
   // molecules (one for fock_ctx_create, many for a batch)
@@ -425,7 +436,10 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   if (c->opt.shard_count < 1 || c->opt.shard_index < 0 || c->opt.shard_index >= c->opt.shard_count)
     return FOCK_ERR_INVALID_ARG;
   const double tau = for_tensor ? 0.0 : c->opt.schwarz_eps;
-  const double tmix = c->opt.mixed_threshold;
+  // density-weighted split: the catalog's FP64 prefix holds the candidates, the
+  // quartets whose bound can reach the threshold with max|D| <= kDensityPlanMax
+  const bool density = !for_tensor && c->opt.mixed_density != 0;
+  const double tmix = density ? c->opt.mixed_threshold / kDensityPlanMax : c->opt.mixed_threshold;
   const bool grouping = c->opt.group_by_contraction != 0;
   PlanCatalog tensor_cat;
   if (for_tensor) {
@@ -435,7 +449,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     c->catalog.valid = true;
   }
   const PlanCatalog& cat = for_tensor ? tensor_cat : c->catalog;
-  const bool ctx_mixed = !for_tensor && c->opt.precision == FOCK_PREC_MIXED;
+  // a tensor plan of a mixed context splits on the Schwarz product alone (no density)
+  const bool ctx_mixed = c->opt.precision == FOCK_PREC_MIXED;
   // plan state of molecule m (see fock_ctx::mol_mode)
   auto mode_of = [&](int m) -> int {
     if (for_tensor || c->mol_mode.empty()) return ctx_mixed ? 1 : 2;
@@ -448,29 +463,43 @@ int build_plan(fock_ctx* c, bool for_tensor) {
 
   std::vector<int> ints;
   std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, off; };
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, split, off; };
   std::vector<Pending> pend;
   fock_stats st{};
   st.shell_pairs = (long long)c->hpairs.size();
   st.prim_pairs = c->nprim_pairs;
   st.function_quartets_unique = cat.function_quartets_unique;
-  std::vector<int> rbra, rbeg, rcnt, kets, rsl;
-  for (const CatGroup& G : cat.groups) {
+  std::vector<int> rbra, rbeg, rcnt, kets, rsl, rsplit;
+  // one launch per class and precision: the catalog's groups of a class (one
+  // per ket primitive-pair count, adjacent in the catalog) are concatenated,
+  // so a warp mixes trip counts only where two groups meet
+  for (size_t g0 = 0; g0 < cat.groups.size();) {
+    size_t g1 = g0 + 1;
+    while (g1 < cat.groups.size() && cat.groups[g1].la == cat.groups[g0].la && cat.groups[g1].lb == cat.groups[g0].lb &&
+           cat.groups[g1].lc == cat.groups[g0].lc && cat.groups[g1].ld == cat.groups[g0].ld)
+      ++g1;
+    const CatGroup& G = cat.groups[g0];
     int hrr = 0, neri = 0;
     const int vrr = class_vrr_flops(G.la, G.lb, G.lc, G.ld, &hrr, &neri);
     for (int prec = 0; prec < (mixed ? 2 : 1); ++prec) {
-      rbra.clear(); rbeg.clear(); rcnt.clear(); kets.clear();
+      rbra.clear(); rbeg.clear(); rcnt.clear(); kets.clear(); rsplit.clear();
       long long q = 0, pq = 0;
-      for (const CatSeg& sg : G.segs) {
-        const int md = mode_of(sg.mol);
+      // classes whose Boys order exceeds kMixedMaxL stay FP64 in mixed mode
+      const bool fp64_class = G.la + G.lb + G.lc + G.ld > kMixedMaxL;
+      for (size_t gi = g0; gi < g1; ++gi)
+      for (const CatSeg& sg : cat.groups[gi].segs) {
+        int md = mode_of(sg.mol);
+        if (md == 1 && fp64_class) md = 2;
         if (md == 0 || (prec == 1 && md == 2)) continue;
         const int base = (int)kets.size();
         const long long* kp = cat.kpre.data() + sg.ket0;
         bool used = false;
         for (long long r = sg.row0; r < sg.row0 + sg.nrow; ++r) {
-          int beg = 0, end = cat.rall[r];
+          int beg = 0, end = cat.rall[r], split = 0;
           if (md == 1) {
-            if (prec == 0) end = cat.r64[r]; else beg = cat.r64[r];
+            if (prec == 0) { end = cat.r64[r]; split = density ? end : 0; }
+            else if (density) split = cat.r64[r];
+            else beg = cat.r64[r];
           }
           if (end <= beg) continue;
           // multi-rank build: every shard keeps the rows of its residue class
@@ -480,6 +509,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
           rbra.push_back(bi);
           rbeg.push_back(base + beg);
           rcnt.push_back(end - beg);
+          rsplit.push_back(split);
           q += end - beg;
           pq += (long long)c->hpairs[bi].nprim * (kp[end] - kp[beg]);
         }
@@ -515,6 +545,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
         rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + per - 1) / per);
       }
       ints.insert(ints.end(), rsl.begin(), rsl.end());
+      P.split = ints.size();
+      ints.insert(ints.end(), rsplit.begin(), rsplit.end());
       P.off = lls.size();
       long long acc = 0;
       for (size_t r = 0; r < rcnt.size(); ++r) { lls.push_back(acc); acc += (long long)rcnt[r] * rsl[r]; }
@@ -524,6 +556,8 @@ int build_plan(fock_ctx* c, bool for_tensor) {
       const long long flops =
           pq * ((long long)vrr + setup_flops(G.la, G.lb, G.lc, G.ld)) + q * ((long long)hrr + 12LL * neri);
       P.p.flops = flops;
+      P.p.flops_pq = (long long)vrr + setup_flops(G.la, G.lb, G.lc, G.ld);
+      P.p.flops_q = (long long)hrr + 12LL * neri;
       pend.push_back(P);
       if (P.p.prec == PREC_FP32) {
         st.shell_quartets_fp32 += q; st.prim_quartets_fp32 += pq; st.flops_fp32 += flops;
@@ -531,11 +565,14 @@ int build_plan(fock_ctx* c, bool for_tensor) {
         st.shell_quartets_fp64 += q; st.prim_quartets_fp64 += pq; st.flops_fp64 += flops;
       }
     }
+    g0 = g1;
   }
   st.shell_quartets_screened = cat.total_shell_quartets - st.shell_quartets_fp64 - st.shell_quartets_fp32;
-  // work-queue counters of persistent launches live after the row offsets
+  // work-queue counters of persistent launches live after the row offsets,
+  // then the work counters of a density-weighted mixed plan
   c->queue_base = lls.size();
-  lls.insert(lls.end(), pend.size() + 1, 0LL);
+  c->split_counts = density && mixed;
+  lls.insert(lls.end(), pend.size() + 1 + (c->split_counts ? 2 * pend.size() : 0), 0LL);
   CK(dalloc(&c->d_plan_int, ints.size()));
   CK(dalloc(&c->d_plan_ll, lls.size()));
   if (!ints.empty()) CK(cudaMemcpy(c->d_plan_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -551,6 +588,11 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.block = c->opt.block_threads;
     P.p.cl.persist_blocks = (!for_tensor && c->opt.persistent) ? -1 : 0;
     P.p.cl.queue = reinterpret_cast<unsigned long long*>(c->d_plan_ll + c->queue_base + c->plans.size());
+    P.p.cl.row_split = c->split_counts ? c->d_plan_int + P.split : nullptr;
+    P.p.cl.wthr = (float)c->opt.mixed_threshold;
+    P.p.cl.counters = c->split_counts ? reinterpret_cast<unsigned long long*>(
+                                            c->d_plan_ll + c->queue_base + pend.size() + 1 + 2 * c->plans.size())
+                                      : nullptr;
     c->plans.push_back(P.p);
   }
   st.launches_per_build = (int)c->plans.size() + 1;
@@ -592,6 +634,9 @@ int compute_schwarz(fock_ctx* c) {
   CK(e);
   // the float Schwarz factor is rounded up so that screening stays conservative
   for (auto& q : c->Q) q = std::nextafter(q, INFINITY);
+  // and kept in the device pair records (density-weighted precision split)
+  for (int p = 0; p < npairs; ++p) c->hpairs[p].Q = c->Q[p];
+  CK(cudaMemcpy(c->d_pairs, c->hpairs.data(), npairs * sizeof(PairInfo), cudaMemcpyHostToDevice));
   return FOCK_OK;
 }
 
@@ -655,6 +700,7 @@ void fock_options_default(fock_options* o) {
   o->shard_index = 0;
   o->shard_count = 1;
   o->level_shift = 0.0;
+  o->mixed_density = 1;
   o->device = 0;
 }
 
@@ -680,6 +726,29 @@ long long fock_launch_count(const fock_ctx* c) { return c ? c->launches : 0; }
 int fock_get_stats(const fock_ctx* c, fock_stats* st) {
   if (!c || !st) return FOCK_ERR_INVALID_ARG;
   *st = c->stats;
+  if (c->split_counts && !c->plans.empty()) {
+    // density-weighted mixed plan: the FP32 / FP64 split is decided per build,
+    // so the work figures are the counts of the last build
+    const size_t np = c->plans.size();
+    std::vector<long long> cnt(2 * np);
+    CK(cudaSetDevice(c->device));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaMemcpy(cnt.data(), c->d_plan_ll + c->queue_base + np + 1, 2 * np * sizeof(long long),
+                  cudaMemcpyDeviceToHost));
+    st->shell_quartets_fp64 = st->shell_quartets_fp32 = 0;
+    st->prim_quartets_fp64 = st->prim_quartets_fp32 = 0;
+    st->flops_fp64 = st->flops_fp32 = 0;
+    for (size_t i = 0; i < np; ++i) {
+      const Plan& p = c->plans[i];
+      const long long q = cnt[2 * i], pq = cnt[2 * i + 1], fl = pq * p.flops_pq + q * p.flops_q;
+      if (p.prec == PREC_FP32) {
+        st->shell_quartets_fp32 += q; st->prim_quartets_fp32 += pq; st->flops_fp32 += fl;
+      } else {
+        st->shell_quartets_fp64 += q; st->prim_quartets_fp64 += pq; st->flops_fp64 += fl;
+      }
+    }
+    st->shell_quartets_screened = c->catalog.total_shell_quartets - st->shell_quartets_fp64 - st->shell_quartets_fp32;
+  }
   return FOCK_OK;
 }
 
@@ -817,7 +886,10 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       P.mol_off = (int)c->mol_off[A.mol];
       P.mol_n = c->mol_nbf[A.mol];
       P.cls = pair_class(A.l, B.l);
-      for (int k = 0; k < 3; ++k) P.AB[k] = A.c[k] - B.c[k];
+      for (int k = 0; k < 3; ++k) {
+        P.AB[k] = A.c[k] - B.c[k];
+        P.ABf[k] = (float)P.AB[k];
+      }
       const double ab2 = P.AB[0] * P.AB[0] + P.AB[1] * P.AB[1] + P.AB[2] * P.AB[2];
       for (int pa = 0; pa < A.nprim; ++pa)
         for (int pb = 0; pb < B.nprim; ++pb) {
@@ -975,6 +1047,11 @@ int fock_set_precision(fock_ctx* c, int precision, double mixed_threshold) {
 // first, so that the small classes fill in behind them: a single small
 // molecule has too few quartets per class to fill 152 SMs on its own), join,
 // G = M + M^T.  Captured once per plan, replayed per build.
+// Work-queue and work counters after the plans' row offsets.
+static size_t counter_elems(const fock_ctx* c) {
+  return c->plans.size() + 1 + (c->split_counts ? 2 * c->plans.size() : 0);
+}
+
 // Class launches of a build, largest first (by model flops).
 static std::vector<int> plan_order(const fock_ctx* c) {
   std::vector<int> order(c->plans.size());
@@ -983,27 +1060,27 @@ static std::vector<int> plan_order(const fock_ctx* c) {
   return order;
 }
 
-static int capture_jk_graph(fock_ctx* c) {
-  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
+// The launches of one Fock build from c->d_D into c->d_G, issued on the
+// capturing stream cs: clear M, re-arm the work queues / counters, FP32 copy
+// of D, the class launches forked over the side streams (largest first),
+// join, G = M + M^T.  *kernels counts the kernel launches.
+static cudaError_t issue_jk_build(fock_ctx* c, cudaStream_t cs, int* kernels) {
   const size_t nn = (size_t)c->total_elems;
-  cudaStream_t cs = c->cap_stream;
   EriArgs a = eri_args(c);
   bool need32 = false;
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
   const std::vector<int> order = plan_order(c);
   const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
-  CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
   cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
-  int kernels = 0;
-  if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); kernels++; }
-  if (e == cudaSuccess && c->opt.persistent)
-    e = cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, (c->plans.size() + 1) * sizeof(long long), cs);
+  if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); (*kernels)++; }
+  if (e == cudaSuccess && (c->opt.persistent || c->split_counts))
+    e = cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, counter_elems(c) * sizeof(long long), cs);
   if (e == cudaSuccess) e = cudaEventRecord(c->fork_ev, cs);
   for (int s = 0; s < nside && e == cudaSuccess; ++s) e = cudaStreamWaitEvent(c->side[s], c->fork_ev, 0);
   for (size_t k = 0; k < order.size() && e == cudaSuccess; ++k) {
     const Plan& p = c->plans[order[k]];
     e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_JK, p.prec, c->side[k % nside]);
-    kernels++;
+    (*kernels)++;
   }
   for (int s = 0; s < nside && e == cudaSuccess; ++s) {
     e = cudaEventRecord(c->join_ev[s], c->side[s]);
@@ -1011,8 +1088,17 @@ static int capture_jk_graph(fock_ctx* c) {
   }
   if (e == cudaSuccess) {
     e = k_symmetrize_blocks(c->d_M, c->d_G, c->d_mol_off, c->d_mol_n, c->nmol, c->total_elems, cs);
-    kernels++;
+    (*kernels)++;
   }
+  return e;
+}
+
+static int capture_jk_graph(fock_ctx* c) {
+  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
+  cudaStream_t cs = c->cap_stream;
+  CK(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+  int kernels = 0;
+  cudaError_t e = issue_jk_build(c, cs, &kernels);
   cudaGraph_t g = nullptr;
   cudaError_t e2 = cudaStreamEndCapture(cs, &g);
   if (e == cudaSuccess) e = e2;
@@ -1050,8 +1136,8 @@ int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, dou
   const size_t nn = (size_t)n * n;
   cudaStream_t cs = c->stream;
   CK(cudaMemsetAsync(M, 0, nn * sizeof(double), cs));
-  if (c->opt.persistent)
-    CK(cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, (c->plans.size() + 1) * sizeof(long long), cs));
+  if (c->opt.persistent || c->split_counts)
+    CK(cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, counter_elems(c) * sizeof(long long), cs));
   EriArgs a = eri_args(c);
   a.D = D_dev;
   a.D32 = D32;
@@ -1254,6 +1340,7 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       int* keep_i = c->d_plan_int;
       long long* keep_l = c->d_plan_ll;
       const size_t keep_q = c->queue_base;
+      const bool keep_split = c->split_counts;
       c->d_plan_int = nullptr;
       c->d_plan_ll = nullptr;
       rc = build_plan(c, true);
@@ -1261,7 +1348,7 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
         EriArgs a = eri_args(c);
         a.tensor = d_t;
         for (const Plan& p : c->plans) {
-          e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_TENSOR, PREC_FP64, c->stream);
+          e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_TENSOR, p.prec, c->stream);
           c->launches++;
           if (e != cudaSuccess) break;
         }
@@ -1272,6 +1359,7 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
       c->d_plan_int = keep_i;
       c->d_plan_ll = keep_l;
       c->queue_base = keep_q;
+      c->split_counts = keep_split;
       c->plans = keep_plans;
       c->opt = keep;
     }
@@ -1443,6 +1531,40 @@ int fock_energy_backward(fock_ctx* c, const fock_scf_result* r, double* grad) {
   return fock_gradient(c, r->density_matrix, W.data(), grad);
 }
 
+int fock_sorted_eigs(int device, int n, const double* A, double* evals, double* evecs) {
+  if (!A || !evals || !evecs || n < 1 || n > kEigMaxN) return FOCK_ERR_INVALID_ARG;
+  for (long long i = 0; i < (long long)n * n; ++i)
+    if (!std::isfinite(A[i])) return FOCK_ERR_INVALID_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return FOCK_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(device));
+  const size_t nn = (size_t)n * n;
+  // row-major symmetric in = column-major symmetric; column-major eigenvectors out
+  double *d_A = nullptr, *d_V = nullptr, *d_w = nullptr, *d_work = nullptr, *d_meta = nullptr;
+  cudaError_t e = dalloc(&d_A, nn);
+  if (e == cudaSuccess) e = dalloc(&d_V, nn);
+  if (e == cudaSuccess) e = dalloc(&d_w, (size_t)n);
+  if (e == cudaSuccess) e = dalloc(&d_work, eig_small_work_elems((long long)nn, n, 1));
+  if (e == cudaSuccess) e = dalloc(&d_meta, 4);
+  const long long lm[2] = {0, 0};
+  const int im[2] = {n, 0};
+  long long* off = reinterpret_cast<long long*>(d_meta);
+  int* nsz = reinterpret_cast<int*>(d_meta + 2);
+  if (e == cudaSuccess) e = cudaMemcpy(d_A, A, nn * 8, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(off, lm, sizeof(lm), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(nsz, im, sizeof(im), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = eig_small(d_A, d_V, d_w, off, off + 1, nsz, nsz + 1, 1, n, d_work, (long long)nn, n, 0);
+  std::vector<double> V(nn);
+  if (e == cudaSuccess) e = cudaMemcpy(V.data(), d_V, nn * 8, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(evals, d_w, (size_t)n * 8, cudaMemcpyDeviceToHost);
+  dfree(d_A); dfree(d_V); dfree(d_w); dfree(d_work); dfree(d_meta);
+  CK(e);
+  for (int i = 0; i < n; ++i)  // row-major evecs[i][k] = component i of eigenvector k
+    for (int k = 0; k < n; ++k) evecs[(size_t)i * n + k] = V[(size_t)k * n + i];
+  return FOCK_OK;
+}
+
 int fock_boys_eval(int device, int form, int order, const double* T, int n, double* out) {
   if (!T || !out || n < 0 || form < FOCK_BOYS_FP64 || form > FOCK_BOYS_MD || order < 0 ||
       order > (form == FOCK_BOYS_REFERENCE ? 10 : kBoysMaxM))
@@ -1548,15 +1670,30 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     if (d_order) cudaFree(d_order);
     if (d_info) cudaFree(d_info);
   };
+  bool init_ok = true;
+  auto cku_init = [&](cudaError_t x) { init_ok = init_ok && x == cudaSuccess; };
   if (!ok) { cleanup(); return FOCK_ERR_OOM; }
   cudaStream_t s = c->stream;
   const double one = 1.0, zero = 0.0, two = 2.0;
+  // eigensolver: the batched small-matrix solver (eigen.cu) up to kEigMaxN
+  // functions, cuSOLVER's dsyevd above
+  const bool small_eig = n <= kEigMaxN;
   int lwork = 0;
-  if (cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U, n, w, &lwork) !=
-      CUSOLVER_STATUS_SUCCESS) { cleanup(); return FOCK_ERR_CUDA; }
-  double* work = mk(lwork);
-  if (!work) { cleanup(); return FOCK_ERR_OOM; }
-  int fail = FOCK_OK;
+  if (!small_eig &&
+      cusolverDnDsyevd_bufferSize(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U, n, w, &lwork) !=
+          CUSOLVER_STATUS_SUCCESS) { cleanup(); return FOCK_ERR_CUDA; }
+  double* work = small_eig ? mk(eig_small_work_elems((long long)nn, n, 1)) : mk(lwork);
+  double* emeta = mk(4);  // eig_small's one-block layout: off, woff (long long), n, list (int)
+  if (!work || !emeta) { cleanup(); return FOCK_ERR_OOM; }
+  long long* e_off = reinterpret_cast<long long*>(emeta);
+  int* e_n = reinterpret_cast<int*>(emeta + 2);
+  if (small_eig) {
+    const long long lm[2] = {0, 0};
+    const int im[2] = {n, 0};
+    cku_init(cudaMemcpyAsync(e_off, lm, sizeof(lm), cudaMemcpyHostToDevice, c->stream));
+    cku_init(cudaMemcpyAsync(e_n, im, sizeof(im), cudaMemcpyHostToDevice, c->stream));
+  }
+  int fail = init_ok ? FOCK_OK : FOCK_ERR_CUDA;
   auto cku = [&](cudaError_t x) { if (x != cudaSuccess && fail == FOCK_OK) fail = map_cuda(x); };
   auto ckb = [&](cublasStatus_t x) { if (x != CUBLAS_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
   auto cks = [&](cusolverStatus_t x) { if (x != CUSOLVER_STATUS_SUCCESS && fail == FOCK_OK) fail = FOCK_ERR_CUDA; };
@@ -1583,19 +1720,29 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       }
     }
   }
+  // eigenvalues into w, eigenvectors of the symmetric Ain into Vout (Ain kept)
+  auto eig = [&](const double* Ain, double* Vout) {
+    if (small_eig) {
+      cku(eig_small(Ain, Vout, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, s));
+      c->launches += eig_small_launches();
+    } else {
+      cku(cudaMemcpyAsync(Vout, Ain, nn * 8, cudaMemcpyDeviceToDevice, s));
+      cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, Vout, n, w, work, lwork,
+                           d_info));
+      c->launches++;
+    }
+  };
   // Loewdin X = U diag(w^-1/2) U^T (scf/src/lib.rs:139-146)
-  cku(cudaMemcpyAsync(U, S, nn * 8, cudaMemcpyDeviceToDevice, s));
-  cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, U, n, w, work, lwork, d_info));
+  eig(S, U);
   cku(k_scale_cols(U, w, W, n, s));
-  c->launches += 2;
+  c->launches++;
   gemm(CUBLAS_OP_N, CUBLAS_OP_T, n, &one, W, U, X);
   std::vector<double> evals(n);
   auto density_from = [&](const double* Fin, double* Dout) {
     gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, &one, X, Fin, T1);  // X^T F
     gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, X, T2);   // X^T F X
-    cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, T2, n, w, work, lwork, d_info));
-    c->launches++;
-    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, X, T2, C);    // C = X C'
+    eig(T2, T1);                                          // C' in T1
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, X, T1, C);    // C = X C'
     if (nocc > 0) {
       ckb(cublasDgemm(c->blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &two, C, n, C, n, &zero, Dout, n));
       c->launches++;
@@ -1607,6 +1754,49 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   c->launches++;
   density_from(F, Dm);
   if (fail != FOCK_OK) { cleanup(); return fail; }
+  // FOCK_GB300_TRACE=1: per-phase host wall times of this SCF on stderr
+  // (set-up; per iteration: Fock build, DIIS algebra, eigensolve + density, energy read-back)
+  const bool trace = std::getenv("FOCK_GB300_TRACE") != nullptr;
+  using clk = std::chrono::steady_clock;
+  double t_ph[4] = {0, 0, 0, 0};
+  if (trace) cudaStreamSynchronize(s);
+  const double t_setup = std::chrono::duration<double>(clk::now() - t_start).count();
+  auto phase = [&](int k, clk::time_point& t0) {
+    if (!trace) return;
+    cudaStreamSynchronize(s);
+    const auto t1 = clk::now();
+    t_ph[k] += std::chrono::duration<double>(t1 - t0).count();
+    t0 = t1;
+  };
+
+  // the result of a finished SCF (energies, D, C, orbital energies)
+  auto fill_result = [&](double e_report, const double* Dfinal, int iter, bool done, double shift_now) {
+    res->electronic_energy = e_report;
+    res->total_energy = e_report + vnn;
+    res->nuclear_repulsion = vnn;
+    res->iterations = iter;
+    res->converged = done ? 1 : 0;
+    res->n_electrons = ne;
+    res->n_basis = n;
+    std::vector<double> hD(nn), hC(nn);
+    if (res->density_matrix || res->coefficient_matrix || res->orbital_energies) {
+      cku(cudaMemcpyAsync(hD.data(), Dfinal, nn * 8, cudaMemcpyDeviceToHost, s));
+      cku(cudaMemcpyAsync(hC.data(), C, nn * 8, cudaMemcpyDeviceToHost, s));
+      cku(cudaMemcpyAsync(evals.data(), w, n * 8, cudaMemcpyDeviceToHost, s));
+      cku(cudaStreamSynchronize(s));
+    }
+    const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
+    if (res->density_matrix)  // symmetric: column-major == row-major
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+          res->density_matrix[(size_t)i * n + j] = hD[(size_t)j * n + i] * (flip ? c->fsign[i] * c->fsign[j] : 1.0);
+    if (res->coefficient_matrix)  // row-major C[i][k] (function i, orbital k)
+      for (int i = 0; i < n; ++i)
+        for (int k = 0; k < n; ++k)
+          res->coefficient_matrix[(size_t)i * n + k] = hC[(size_t)k * n + i] * (flip ? c->fsign[i] : 1.0);
+    if (res->orbital_energies)  // the level shift lifted the virtual orbitals by b
+      for (int k = 0; k < n; ++k) res->orbital_energies[k] = evals[k] - (k >= nocc ? shift_now : 0.0);
+  };
 
   std::vector<int> order;  // slots, oldest first
   int next_slot = 0;
@@ -1623,12 +1813,149 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   const bool mixed = c->opt.precision == FOCK_PREC_MIXED;
   const double mixed_th = c->opt.mixed_threshold;
   bool fp64_phase = false;
-  for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
+
+  // ---- device-driven iterations (small matrices, exact ERIs): every phase of
+  // the loop (mixed, then FP64; or FP64 alone) is one CUDA graph whose
+  // conditional WHILE node runs one RHF iteration per pass of its body --
+  // Fock build, DIIS, level shift, eigensolve, density, energies -- and whose
+  // last kernels decide on the device whether to go on (ks_control), so the
+  // host waits once per phase instead of once per iteration.  The decisions
+  // are the host loop's below, in the same order.
+  bool graph_done = false;
+  if (small_eig && !refc && fail == FOCK_OK) {
+    double* Ecur = mk(nn);
+    ScfDevState* dst = reinterpret_cast<ScfDevState*>(mk((sizeof(ScfDevState) + 7) / 8));
+    if (!Ecur || !dst) { cleanup(); return FOCK_ERR_OOM; }
+    ScfDevState hst{};
+    hst.ring = ring;
+    hst.diis_start = c->opt.diis_start;
+    hst.max_iters = c->opt.max_iters;
+    hst.conv_mode = c->opt.conv_mode == FOCK_CONV_COMMUTATOR ? 0 : 1;
+    hst.final_fp64 = c->opt.final_fp64;
+    hst.epsilon = c->opt.epsilon;
+    hst.shift = c->opt.level_shift;
+    hst.shift_fade = kShiftFade;
+    hst.mixed_switch = kMixedSwitch;
+    hst.stall_err = kMixedStallErr;
+    hst.stall_max = kMixedStall;
+    hst.err_prev = 1.0;
+    hst.err_best = 1e300;
+    // the build reads c->d_D and writes c->d_G: the loop's density lives there
+    double* Dg = c->d_D;
+    double* Gg = c->d_G;
+    cku(cudaMemcpyAsync(Dg, Dm, nn * 8, cudaMemcpyDeviceToDevice, s));
+    int per_iter = 0;  // kernels of one iteration
+    for (int ph = 0; ph < 2 && fail == FOCK_OK; ++ph) {
+      hst.mixed_phase = (mixed && c->opt.final_fp64 && !fp64_phase) ? 1 : 0;
+      if (ph == 0) cku(cudaMemcpyAsync(dst, &hst, sizeof(hst), cudaMemcpyHostToDevice, s));
+      else cku(cudaMemcpyAsync(&dst->mixed_phase, &hst.mixed_phase, sizeof(int), cudaMemcpyHostToDevice, s));
+      cku(cudaStreamSynchronize(s));
+      if (fail != FOCK_OK) break;
+      cudaGraph_t g = nullptr, body = nullptr;
+      cudaGraphExec_t ge = nullptr;
+      cudaGraphConditionalHandle h;
+      cudaError_t e = cudaGraphCreate(&g, 0);
+      if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+      cudaGraphNodeParams cp{};
+      cp.type = cudaGraphNodeTypeConditional;
+      cp.conditional.handle = h;
+      cp.conditional.type = cudaGraphCondTypeWhile;
+      cp.conditional.size = 1;
+      cudaGraphNode_t node;
+      if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp);
+      cudaStream_t cs = c->cap_stream;
+      if (e == cudaSuccess) {
+        body = cp.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+      }
+      if (e == cudaSuccess) {
+        int kn = 0;
+        auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
+        auto gm = [&](bool ta, bool tb, double alpha, int kd, const double* A, const double* B, double* Cc) {
+          ck(gemm_blocks(ta, tb, alpha, kd, A, B, Cc, e_off, e_n, e_n + 1, 1, n, cs));
+          kn++;
+        };
+        ck(ks_iter_begin(dst, cs));
+        ck(issue_jk_build(c, cs, &kn));
+        ck(ks_build_done(dst, cs));
+        ck(k_add(H, Gg, F, (int)nn, cs));
+        ck(cudaMemsetAsync(scal, 0, 4 * 8, cs));
+        ck(k_energy(Dg, H, Gg, (int)nn, scal, cs));            // consistent energy of D
+        gm(false, false, 1.0, -1, F, Dg, T1);                  // F D
+        gm(false, false, 1.0, -1, T1, S, T2);                  // F D S
+        ck(k_commutator(T2, Ecur, n, (unsigned long long*)(scal + 2), cs));
+        ck(ks_store_slot(dst, Ecur, Ering, (int)nn, cs));
+        ck(ks_store_slot(dst, F, Fring, (int)nn, cs));
+        ck(ks_diis_dots(Ering, (int)nn, dst, ring, Bm, cs));
+        ck(ks_diis_solve(Bm, ring, dst, coef, cs));
+        ck(ks_diis_extrapolate(Fring, (int)nn, dst, coef, ring, Fd, cs));
+        kn += 10;
+        const double* Fuse = Fd;
+        if (c->opt.level_shift != 0.0) {  // F + b (S - 1/2 S D S)
+          gm(false, false, 1.0, -1, S, Dg, T1);
+          gm(false, false, 1.0, -1, T1, S, T2);
+          ck(ks_level_shift(Fd, S, T2, dst, (long long)nn, Fsh, cs));
+          kn++;
+          Fuse = Fsh;
+        }
+        gm(true, false, 1.0, -1, X, Fuse, T1);                 // X^T F
+        gm(false, false, 1.0, -1, T1, X, T2);                  // X^T F X
+        ck(eig_small(T2, T1, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, cs));
+        kn += eig_small_launches();
+        gm(false, false, 1.0, -1, X, T1, C);                   // C = X C'
+        if (nocc > 0) gm(false, true, 2.0, nocc, C, C, Dn);    // D = 2 C_occ C_occ^T
+        else ck(cudaMemsetAsync(Dn, 0, nn * 8, cs));
+        ck(k_energy(Dn, H, Gg, (int)nn, scal + 1, cs));        // reference energy: new D, old G
+        ck(ks_control(dst, scal, h, cs));
+        ck(ks_copy_density(dst, Dn, Dg, (int)nn, cs));
+        kn += 3;
+        per_iter = kn;
+        cudaGraph_t out = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(cs, &out);
+        if (e == cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&ge, g, 0);
+      if (e == cudaSuccess) e = cudaGraphLaunch(ge, s);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(&hst, dst, sizeof(hst), cudaMemcpyDeviceToHost, s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+      if (ge) cudaGraphExecDestroy(ge);
+      if (g) cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        cudaGetLastError();  // clear a non-sticky error before reporting it
+        fail = map_cuda(e);
+        break;
+      }
+      graph_done = true;
+      if (hst.outcome == 2) {  // mixed phase finished: the remaining iterations in FP64
+        int r = fock_set_precision(c, FOCK_PREC_FP64, c->opt.mixed_threshold);
+        if (r != FOCK_OK) { fail = r; break; }
+        fp64_phase = true;
+        continue;
+      }
+      break;
+    }
+    if (graph_done && fail == FOCK_OK) {
+      builds = hst.builds;
+      fock_ms = 1e-6 * (double)hst.build_ns;
+      c->launches += (long long)per_iter * hst.builds;
+      if (hst.outcome == 1) {
+        fill_result(c->opt.energy_mode == 0 ? hst.e_ref : hst.e_cur, c->opt.energy_mode == 0 ? Dn : Dg, hst.iter,
+                    hst.converged != 0, hst.shift_now);
+        result = FOCK_OK;
+      } else {
+        result = FOCK_ERR_DIVERGED;
+      }
+    }
+  }
+
+  for (int iter = 0; !graph_done && iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
+    auto tp = clk::now();
     cudaEventRecord(ev0, s);
     if (refc) { cku(md_g_from_tensor(c->d_tensor, Dm, n, G, s)); c->launches++; }
     else { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
     builds++;
+    phase(0, tp);
     cku(k_add(H, G, F, (int)nn, s));
     cku(cudaMemsetAsync(scal, 0, 4 * 8, s));
     cku(k_energy(Dm, H, G, (int)nn, scal, s));            // consistent energy of Dm
@@ -1659,12 +1986,15 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       c->launches++;
       Fuse = Fsh;
     }
+    phase(1, tp);
     density_from(Fuse, Dn);
+    phase(2, tp);
     cku(k_energy(Dn, H, G, (int)nn, scal + 1, s));        // reference energy: new D, old G
     c->launches++;
     double hs[4];
     cku(cudaMemcpyAsync(hs, scal, 4 * 8, cudaMemcpyDeviceToHost, s));
     cku(cudaStreamSynchronize(s));
+    phase(3, tp);
     if (fail != FOCK_OK) break;
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ev0, ev1);
@@ -1692,33 +2022,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       continue;
     }
     if (done || iter == c->opt.max_iters) {
-      double e_report = c->opt.energy_mode == 0 ? e_ref : e_cur;
-      const double* Dfinal = c->opt.energy_mode == 0 ? Dn : Dm;
-      res->electronic_energy = e_report;
-      res->total_energy = e_report + vnn;
-      res->nuclear_repulsion = vnn;
-      res->iterations = iter;
-      res->converged = done ? 1 : 0;
-      res->n_electrons = ne;
-      res->n_basis = n;
-      std::vector<double> hD(nn), hC(nn);
-      if (res->density_matrix || res->coefficient_matrix || res->orbital_energies) {
-        cku(cudaMemcpyAsync(hD.data(), Dfinal, nn * 8, cudaMemcpyDeviceToHost, s));
-        cku(cudaMemcpyAsync(hC.data(), C, nn * 8, cudaMemcpyDeviceToHost, s));
-        cku(cudaMemcpyAsync(evals.data(), w, n * 8, cudaMemcpyDeviceToHost, s));
-        cku(cudaStreamSynchronize(s));
-      }
-      const bool flip = c->opt.sign_convention == FOCK_SIGN_REFERENCE;
-      if (res->density_matrix)  // symmetric: column-major == row-major
-        for (int i = 0; i < n; ++i)
-          for (int j = 0; j < n; ++j)
-            res->density_matrix[(size_t)i * n + j] = hD[(size_t)j * n + i] * (flip ? c->fsign[i] * c->fsign[j] : 1.0);
-      if (res->coefficient_matrix)  // row-major C[i][k] (function i, orbital k)
-        for (int i = 0; i < n; ++i)
-          for (int k = 0; k < n; ++k)
-            res->coefficient_matrix[(size_t)i * n + k] = hC[(size_t)k * n + i] * (flip ? c->fsign[i] : 1.0);
-      if (res->orbital_energies)  // the level shift lifted the virtual orbitals by b
-        for (int k = 0; k < n; ++k) res->orbital_energies[k] = evals[k] - (k >= nocc ? shift_now : 0.0);
+      fill_result(c->opt.energy_mode == 0 ? e_ref : e_cur, c->opt.energy_mode == 0 ? Dn : Dm, iter, done, shift_now);
       result = FOCK_OK;
       break;
     }
@@ -1732,6 +2036,14 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   res->fock_seconds = fock_ms * 1e-3;
   res->fock_builds = builds;
   res->scf_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  if (trace && graph_done)
+    std::fprintf(stderr, "fock_scf trace: n %d, %d builds, setup %.2f ms, device-driven iterations %.2f ms "
+                 "(builds %.2f ms), total %.2f ms\n", n, builds, 1e3 * t_setup, 1e3 * (res->scf_seconds - t_setup),
+                 fock_ms, 1e3 * res->scf_seconds);
+  else if (trace)
+    std::fprintf(stderr, "fock_scf trace: n %d, %d builds, setup %.2f ms, build %.2f ms, algebra %.2f ms, "
+                 "eigensolve+density %.2f ms, read-back %.2f ms, total %.2f ms\n", n, builds, 1e3 * t_setup,
+                 1e3 * t_ph[0], 1e3 * t_ph[1], 1e3 * t_ph[2], 1e3 * t_ph[3], 1e3 * res->scf_seconds);
   cleanup();
   if (fail != FOCK_OK) return fail;
   return result;
@@ -1933,10 +2245,29 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
                                   &zero, Cc + r.off, r.n, st, r.cnt));
     c->launches++;
   };
+  // eigensolver: molecules of up to kEigMaxN functions in one eig_small call
+  // over the active ones (eigen.cu); larger ones in cuSOLVER's batched syev
+  int nmax_small = 0;
+  for (const Run& r : runs)
+    if (r.n <= kEigMaxN) nmax_small = std::max(nmax_small, r.n);
+  double* ework = nmax_small > 0 ? (double*)mk(eig_small_work_elems(T, woff[nmol], nmol) * 8) : nullptr;
+  int* d_elist = (int*)mk((size_t)nmol * sizeof(int));
+  int n_elist = 0;
+  std::vector<int> elist;
+  auto upload_elist = [&]() {  // the active molecules that eig_small takes
+    elist.clear();
+    for (const Run& r : act)
+      if (r.n <= kEigMaxN)
+        for (int k = r.m0; k < r.m0 + r.cnt; ++k) elist.push_back(k);
+    n_elist = (int)elist.size();
+    if (n_elist > 0)
+      cku(cudaMemcpyAsync(d_elist, elist.data(), n_elist * sizeof(int), cudaMemcpyHostToDevice, s));
+  };
   cusolverDnParams_t sp = nullptr;
   cks(cusolverDnCreateParams(&sp));
   size_t dws = 0, hws = 0;
   for (const Run& r : runs) {
+    if (r.n <= kEigMaxN) continue;
     size_t d1 = 0, h1 = 0;
     cks(cusolverDnXsyevBatched_bufferSize(c->solver, sp, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, r.n,
                                           CUDA_R_64F, U + r.off, r.n, CUDA_R_64F, w + r.woff, CUDA_R_64F, &d1, &h1,
@@ -1949,8 +2280,17 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   if (!ok) { if (sp) cusolverDnDestroyParams(sp); cleanup(); return FOCK_ERR_OOM; }
   const bool trace_syev = std::getenv("FOCK_GB300_TRACE") != nullptr;
   int syev_calls = 0;
-  auto syev = [&](double* A) {  // eigenvectors in place, eigenvalues into w
+  // eigenvalues into w, eigenvectors of the symmetric blocks of Ain into Vout (Ain kept)
+  auto eig = [&](const double* Ain, double* Vout) {
+    if (n_elist > 0) {
+      cku(eig_small(Ain, Vout, w, c->d_mol_off, d_woff, c->d_mol_n, d_elist, n_elist, nmax_small, ework, T,
+                    woff[nmol], s));
+      c->launches += eig_small_launches();
+    }
     for (const Run& r : act) {
+      if (r.n <= kEigMaxN) continue;
+      cku(cudaMemcpyAsync(Vout + r.off, Ain + r.off, (size_t)r.cnt * r.n * r.n * 8, cudaMemcpyDeviceToDevice, s));
+      double* A = Vout;
       const bool sample = trace_syev && (syev_calls % 97) == 0;
       if (sample) cudaStreamSynchronize(s);
       const auto t0 = std::chrono::steady_clock::now();
@@ -1968,16 +2308,16 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     }
   };
   // Loewdin X = U diag(w^-1/2) U^T
-  cku(cudaMemcpyAsync(U, S, TB, cudaMemcpyDeviceToDevice, s));
-  syev(U);
+  upload_elist();
+  eig(S, U);
   cku(kb_scale_cols(U, w, d_woff, c->d_mol_off, c->d_mol_n, nmol, T, W, s));
   c->launches++;
   for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.n, &one, W, U, X);
   auto density_from = [&](const double* Fin, double* Dout) {
     for (const Run& r : act) gemm(r, CUBLAS_OP_T, CUBLAS_OP_N, r.n, &one, X, Fin, T1);
     for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, X, T2);
-    syev(T2);
-    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T2, Cm);
+    eig(T2, T1);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T1, Cm);
     for (const Run& r : act) {
       if (r.nocc > 0) {
         gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.nocc, &two, Cm, Cm, Dout);
@@ -2149,7 +2489,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       if (done[k]) ++n_stale;
     }
     if (ndone == nmol) break;
-    if (ndone != ndone_act) { rebuild_active(); ndone_act = ndone; }
+    if (ndone != ndone_act) { rebuild_active(); upload_elist(); ndone_act = ndone; }
     if ((n_mixed > 0 && n_ready == n_mixed) || n_ready + n_stale >= std::max(1, n_in / 4)) {
       for (int k = 0; k < nmol; ++k) {
         if (done[k]) mode[k] = 0;

@@ -498,4 +498,204 @@ cudaError_t kb_guess(const double* S, const double* H, const long long* off, con
   return cudaGetLastError();
 }
 
+
+// ---------------------------------------------------------------------------
+// Device-driven RHF loop (see ScfDevState): the host loop of fock_scf
+// restated on the device, one iteration per execution of a conditional
+// graph body.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// DIIS ring: slot = iteration mod ring, the last min(iter + 1, ring) slots in
+// use, oldest first (the host loop's round-robin order); level shift of this
+// iteration from the previous DIIS error.
+__global__ void iter_begin_kernel(ScfDevState* st) {
+  const int it = st->iter, ring = st->ring;
+  st->slot = it % ring;
+  const int nused = it + 1 < ring ? it + 1 : ring;
+  st->nused = nused;
+  for (int i = 0; i < nused; ++i) st->order[i] = (it - nused + 1 + i + ring * 2) % ring;
+  st->shift_now = st->shift * fmin(1.0, st->err_prev / st->shift_fade);
+  st->t0 = global_ns();
+}
+
+__global__ void build_done_kernel(ScfDevState* st) {
+  st->build_ns += global_ns() - st->t0;
+  st->builds += 1;
+}
+
+__global__ void diis_dots_st_kernel(const double* Ering, int nn, const ScfDevState* st, int ring, double* B) {
+  const int k = blockIdx.x;
+  const int slot = st->slot;
+  if (k >= st->nused) return;
+  const double* a = Ering + (size_t)slot * nn;
+  const double* b = Ering + (size_t)k * nn;
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < nn; t += blockDim.x) acc += a[t] * b[t];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sm[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) sm[w] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sm[i];
+    B[slot * ring + k] = s;
+    B[k * ring + slot] = s;
+  }
+}
+
+// as diis_solve_kernel over the state's slots; coef[ring] = 1 when the
+// extrapolation applies (enough vectors and a regular system), 0 otherwise
+__global__ void diis_solve_st_kernel(const double* B, int ring, const ScfDevState* st, double* coef) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int m = st->nused;
+  if (m < st->diis_start) { coef[ring] = 0.0; return; }
+  double A[17 * 17], rhs[17];
+  const int M = m + 1;
+  for (int i = 0; i < m; ++i) {
+    for (int j = 0; j < m; ++j) A[i * M + j] = B[st->order[i] * ring + st->order[j]];
+    A[i * M + m] = -1.0;
+    A[m * M + i] = -1.0;
+    rhs[i] = 0.0;
+  }
+  A[m * M + m] = 0.0;
+  rhs[m] = -1.0;
+  bool ok = true;
+  for (int c = 0; c < M && ok; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < M; ++r)
+      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
+    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
+    if (piv != c) {
+      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
+      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
+    }
+    for (int r = c + 1; r < M; ++r) {
+      const double f = A[r * M + c] / A[c * M + c];
+      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
+      rhs[r] -= f * rhs[c];
+    }
+  }
+  if (ok) {
+    for (int c = M - 1; c >= 0; --c) {
+      double s = rhs[c];
+      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
+      rhs[c] = s / A[c * M + c];
+      if (!isfinite(rhs[c])) ok = false;
+    }
+  }
+  for (int i = 0; i < m; ++i) coef[i] = ok ? rhs[i] : 0.0;
+  coef[ring] = ok ? 1.0 : 0.0;
+}
+
+__global__ void diis_extrapolate_st_kernel(const double* Fring, int nn, const ScfDevState* st, const double* coef,
+                                           int ring, double* Fd) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn) return;
+  if (coef[ring] == 0.0) { Fd[t] = Fring[(size_t)st->slot * nn + t]; return; }
+  double acc = 0.0;
+  for (int i = 0; i < st->nused; ++i) acc += coef[i] * Fring[(size_t)st->order[i] * nn + t];
+  Fd[t] = acc;
+}
+
+__global__ void level_shift_st_kernel(const double* F, const double* S, const double* SDS, const ScfDevState* st,
+                                      long long nn, double* out) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nn) return;
+  const double b = st->shift_now;
+  out[t] = F[t] + b * (S[t] - 0.5 * SDS[t]);
+}
+
+// The decisions of the host loop, in its order: mixed-phase switch to FP64,
+// convergence or the iteration limit, divergence, else the next iteration.
+__global__ void control_kernel(ScfDevState* st, const double* scal, cudaGraphConditionalHandle h) {
+  const double e_cur = scal[0], e_ref = scal[1];
+  const double err = __longlong_as_double((long long)(*reinterpret_cast<const unsigned long long*>(scal + 2)));
+  st->e_cur = e_cur;
+  st->e_ref = e_ref;
+  st->err = err;
+  st->err_prev = err;
+  const int it = st->iter;
+  bool done;
+  if (st->conv_mode == 0) done = err < st->epsilon;
+  else done = it > 0 && fabs(e_cur - st->e_prev) < st->epsilon && err < sqrt(st->epsilon);
+  if (err < 0.5 * st->err_best) { st->err_best = err; st->stall = 0; } else { st->stall += 1; }
+  const bool floor = st->stall >= st->stall_max && err < st->stall_err;
+  int outcome = 0;
+  if (st->mixed_phase && st->final_fp64 && (done || err < st->mixed_switch || floor || it >= st->max_iters / 2) &&
+      it < st->max_iters)
+    outcome = 2;
+  else if (done || it == st->max_iters)
+    outcome = 1;
+  else if (!isfinite(err))
+    outcome = 3;
+  st->converged = (outcome == 1 && done) ? 1 : 0;
+  st->outcome = outcome;
+  // the next iteration starts from the new density (also across the switch)
+  st->copy_density = (outcome == 0 || outcome == 2) ? 1 : 0;
+  if (outcome == 0 || outcome == 2) {
+    st->e_prev = e_cur;
+    st->iter = it + 1;
+  }
+  cudaGraphSetConditional(h, outcome == 0 ? 1u : 0u);
+}
+
+__global__ void store_slot_kernel(const ScfDevState* st, const double* src, double* ring, int nn) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nn) ring[(size_t)st->slot * nn + t] = src[t];
+}
+
+__global__ void copy_density_kernel(const ScfDevState* st, const double* Dn, double* Dm, int nn) {
+  if (!st->copy_density) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < nn) Dm[t] = Dn[t];
+}
+
+}  // namespace
+
+cudaError_t ks_iter_begin(ScfDevState* st, cudaStream_t s) {
+  iter_begin_kernel<<<1, 1, 0, s>>>(st);
+  return cudaGetLastError();
+}
+cudaError_t ks_build_done(ScfDevState* st, cudaStream_t s) {
+  build_done_kernel<<<1, 1, 0, s>>>(st);
+  return cudaGetLastError();
+}
+cudaError_t ks_diis_dots(const double* Ering, int nn, const ScfDevState* st, int ring, double* B, cudaStream_t s) {
+  diis_dots_st_kernel<<<ring, 256, 0, s>>>(Ering, nn, st, ring, B);
+  return cudaGetLastError();
+}
+cudaError_t ks_diis_solve(const double* B, int ring, const ScfDevState* st, double* coef, cudaStream_t s) {
+  diis_solve_st_kernel<<<1, 32, 0, s>>>(B, ring, st, coef);
+  return cudaGetLastError();
+}
+cudaError_t ks_diis_extrapolate(const double* Fring, int nn, const ScfDevState* st, const double* coef, int ring,
+                                double* Fd, cudaStream_t s) {
+  diis_extrapolate_st_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(Fring, nn, st, coef, ring, Fd);
+  return cudaGetLastError();
+}
+cudaError_t ks_level_shift(const double* F, const double* S, const double* SDS, const ScfDevState* st, long long nn,
+                           double* out, cudaStream_t s) {
+  level_shift_st_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(F, S, SDS, st, nn, out);
+  return cudaGetLastError();
+}
+cudaError_t ks_store_slot(const ScfDevState* st, const double* src, double* ring, int nn, cudaStream_t s) {
+  store_slot_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(st, src, ring, nn);
+  return cudaGetLastError();
+}
+cudaError_t ks_control(ScfDevState* st, const double* scal, cudaGraphConditionalHandle h, cudaStream_t s) {
+  control_kernel<<<1, 1, 0, s>>>(st, scal, h);
+  return cudaGetLastError();
+}
+cudaError_t ks_copy_density(const ScfDevState* st, const double* Dn, double* Dm, int nn, cudaStream_t s) {
+  copy_density_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(st, Dn, Dm, nn);
+  return cudaGetLastError();
+}
 }  // namespace fockgb

@@ -43,3 +43,38 @@ cudaError_t kb_scale_cols(const double* U, const double* w, const long long* wof
 cudaError_t kb_guess(const double* S, const double* H, const long long* off, const int* n, int nmol, long long total,
                      int gwh, double* F, cudaStream_t s);
 }  // namespace fockgb
+
+namespace fockgb {
+// State of a device-driven RHF loop (one molecule): the iteration's bookkeeping
+// that the host loop keeps in variables, so that one CUDA graph with a
+// conditional WHILE node can run the iterations without host round trips.
+struct ScfDevState {
+  // settings (written by the host before the loop)
+  int ring, diis_start, max_iters, conv_mode, mixed_phase, final_fp64;
+  double epsilon, shift, shift_fade, mixed_switch, stall_err;
+  int stall_max;
+  // per-iteration state
+  int iter, slot, nused, order[16];
+  double shift_now, err, err_prev, err_best, e_cur, e_ref, e_prev;
+  int stall, builds;
+  unsigned long long t0, build_ns;
+  // outcome: 1 = converged / hit max_iters (result), 2 = switch to FP64, 3 = diverged
+  int outcome, converged, copy_density;
+};
+
+// Kernels of one iteration of the device-driven loop (scf_device.cu).
+cudaError_t ks_iter_begin(ScfDevState* st, cudaStream_t s);
+cudaError_t ks_build_done(ScfDevState* st, cudaStream_t s);
+cudaError_t ks_diis_dots(const double* Ering, int nn, const ScfDevState* st, int ring, double* B, cudaStream_t s);
+cudaError_t ks_diis_solve(const double* B, int ring, const ScfDevState* st, double* coef, cudaStream_t s);
+cudaError_t ks_diis_extrapolate(const double* Fring, int nn, const ScfDevState* st, const double* coef, int ring,
+                                double* Fd, cudaStream_t s);
+cudaError_t ks_level_shift(const double* F, const double* S, const double* SDS, const ScfDevState* st, long long nn,
+                           double* out, cudaStream_t s);
+// ring[slot] <- src (the slot of this iteration)
+cudaError_t ks_store_slot(const ScfDevState* st, const double* src, double* ring, int nn, cudaStream_t s);
+// convergence / switch / stop decision; sets the WHILE condition of the loop
+cudaError_t ks_control(ScfDevState* st, const double* scal, cudaGraphConditionalHandle h, cudaStream_t s);
+// Dm <- Dn when the loop continues (st->copy_density)
+cudaError_t ks_copy_density(const ScfDevState* st, const double* Dn, double* Dm, int nn, cudaStream_t s);
+}  // namespace fockgb

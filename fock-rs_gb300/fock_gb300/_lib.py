@@ -43,7 +43,8 @@ class Options(C.Structure):
                 ("energy_mode", C.c_int), ("final_fp64", C.c_int), ("device", C.c_int),
                 ("prims_per_slice", C.c_int), ("prims_per_slice_fp32", C.c_int),
                 ("block_threads", C.c_int), ("persistent", C.c_int),
-                ("shard_index", C.c_int), ("shard_count", C.c_int), ("level_shift", C.c_double)]
+                ("shard_index", C.c_int), ("shard_count", C.c_int), ("level_shift", C.c_double),
+                ("mixed_density", C.c_int)]
 
 
 class ScfResult(C.Structure):
@@ -124,6 +125,7 @@ def lib():
         L.fock_strerror.restype = C.c_char_p
         L.fock_measure_fma_peak.argtypes = [C.c_int, C.c_int, dp]
         L.fock_boys_eval.argtypes = [C.c_int, C.c_int, C.c_int, dp, C.c_int, dp]
+        L.fock_sorted_eigs.argtypes = [C.c_int, C.c_int, dp, dp, dp]
         L.fock_profile_build.argtypes = [vp, vp, C.POINTER(LaunchProfile), C.c_int]
         L.fock_autotune.argtypes = [vp, vp, C.c_int, C.POINTER(Tuning)]
         L.fock_set_tuning.argtypes = [vp, C.POINTER(Tuning)]

@@ -44,7 +44,8 @@ extern "C" {
 #define FOCK_SIGN_STANDARD 1  /* phi ~ (r - A)^l */
 
 #define FOCK_PREC_FP64 0  /* plain: every quartet in FP64 */
-#define FOCK_PREC_MIXED 1 /* FP32 where Q_ab Q_cd < mixed_threshold, FP64 otherwise */
+#define FOCK_PREC_MIXED 1 /* FP32 where the quartet's bound is below mixed_threshold, FP64 otherwise
+                             (see mixed_density); classes with la+lb+lc+ld > 6 always FP64 */
 
 #define FOCK_ERI_EXACT 0     /* accurate Boys, correct recursions (the product path) */
 #define FOCK_ERI_REFCOMPAT 1 /* reference Boys LUT + x-branch recursion defect + 1e-6 zeroing
@@ -106,6 +107,10 @@ typedef struct {
                                batches), so the last iterations are plain DIIS.  Self-consistent
                                solutions are unchanged; reported orbital energies are unshifted.
                                0 = the reference's loop. */
+  int mixed_density;        /* FOCK_PREC_MIXED: 1 = a shell quartet runs in FP64 when
+                               Q_ab Q_cd max|D| >= mixed_threshold, max|D| over the six density
+                               blocks it is contracted with (the density of each build); 0 = when
+                               Q_ab Q_cd >= mixed_threshold (Schwarz product alone) */
 } fock_options;
 
 typedef struct {
@@ -127,8 +132,9 @@ typedef struct {
 typedef struct fock_ctx fock_ctx;
 
 /* Defaults: reference sign convention, FP64, exact ERIs, schwarz 1e-12,
- * mixed threshold 1.0, prim_eps 1e-20, grouping on, SCF 100 iterations,
- * epsilon 1e-6, commutator convergence, GWH guess, DIIS 16/5, energy_mode 0. */
+ * mixed threshold 1.0 with density weighting, prim_eps 1e-20, grouping on,
+ * SCF 100 iterations, epsilon 1e-6, commutator convergence, GWH guess,
+ * DIIS 16/5, energy_mode 0. */
 void fock_options_default(fock_options* opt);
 
 /* Build shell pairs and primitive-pair data, Schwarz factors and the
@@ -144,7 +150,9 @@ int fock_set_precision(fock_ctx* ctx, int precision, double mixed_threshold);
 
 /* Full symmetric N^4 tensor, out[((l*N + k)*N + j)*N + i] = (ij|kl), so that
  * out is indexed like ElectronTensor's Index (electron_tensor.rs:179-187).
- * Debug / parity path; N <= 160. */
+ * Debug / parity path; N <= 160.  With FOCK_PREC_MIXED, the shell quartets
+ * with Q_ab Q_cd < mixed_threshold are computed by the FP32 kernels (the
+ * per-integral error of the mixed path; no density weighting here). */
 int fock_eri_tensor(fock_ctx* ctx, double* out_n4);
 
 /* G = J - K/2 for a symmetric density D (host arrays), the two-electron part
@@ -262,6 +270,9 @@ typedef struct {
   long long flops_fp32;
   int launches_per_build;
 } fock_stats;
+/* With a density-weighted mixed plan (mixed_density = 1) the FP32 / FP64 split
+ * is decided in every build, so the quartet, primitive-quartet and flop figures
+ * are those the last build computed (zero before the first build). */
 int fock_get_stats(const fock_ctx* ctx, fock_stats* st);
 
 /* Per-launch profile of one Fock build from a device density: every class
@@ -316,6 +327,12 @@ int fock_set_tuning(fock_ctx* ctx, const fock_tuning* t);
 int fock_batch_autotune(fock_batch* batch, const double* D_dev, int reps, fock_tuning* best);
 
 const char* fock_strerror(int code);
+
+/* sorted_eigs (scf/src/utils.rs:59-99): eigenvalues of the symmetric n x n
+ * row-major A in ascending order and the matching orthonormal eigenvectors,
+ * evecs[i * n + k] = component i of eigenvector k, by the device eigensolver
+ * of the SCF (FP32 Jacobi refined to FP64 accuracy); n <= 128. */
+int fock_sorted_eigs(int device, int n, const double* A, double* evals, double* evecs);
 
 /* The device Boys functions F_0(t)..F_order(t) at n host arguments t >= 0,
  * out[i * (order + 1) + m] = F_m(T[i]), evaluated on the device by the same
