@@ -1822,7 +1822,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   // host waits once per phase instead of once per iteration.  The decisions
   // are the host loop's below, in the same order.
   bool graph_done = false;
-  if (small_eig && !refc && fail == FOCK_OK) {
+  if (small_eig && !refc && c->opt.max_iters >= 0 && fail == FOCK_OK) {
     double* Ecur = mk(nn);
     ScfDevState* dst = reinterpret_cast<ScfDevState*>(mk((sizeof(ScfDevState) + 7) / 8));
     if (!Ecur || !dst) { cleanup(); return FOCK_ERR_OOM; }

@@ -632,7 +632,7 @@ __global__ void control_kernel(ScfDevState* st, const double* scal, cudaGraphCon
   if (st->mixed_phase && st->final_fp64 && (done || err < st->mixed_switch || floor || it >= st->max_iters / 2) &&
       it < st->max_iters)
     outcome = 2;
-  else if (done || it == st->max_iters)
+  else if (done || it >= st->max_iters)  // >=: the loop ends whatever max_iters is
     outcome = 1;
   else if (!isfinite(err))
     outcome = 3;
