@@ -484,11 +484,17 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
   }
 }
 
-// Gradient launch of the classes whose analytic derivative recurrences are
-// not generated (finite-difference kernel, eri_grad_fd.cuh); defined and
-// instantiated in translation units of their own (gen/inst_fd_*.cu).
+// Gradient launch of the classes whose derivative recurrences are not
+// generated (the classes with d shells): dual-number differentiation of the
+// class's own recurrences (eri_grad_ad.cuh); defined and instantiated in
+// translation units of their own (gen/inst_ad_*.cu).
+template <class C>
+cudaError_t launch_grad_ad(const ClassLaunch& cl, const EriArgs& a, cudaStream_t s);
+// (dd|dd), whose dual-number form compiles for minutes: the fourth-order finite
+// difference of the class's integrals (eri_grad_fd.cuh, gen/inst_fd_2222.cu)
 template <class C>
 cudaError_t launch_grad_fd(const ClassLaunch& cl, const EriArgs& a, cudaStream_t s);
+constexpr int kGradAdMaxL = 7;  // equal to the generator's AD_LMAX
 
 // Launch pieces of one class.  The large classes instantiate each piece in a
 // translation unit of its own (gen/inst_*_p<k>.cu, declared extern in
@@ -516,7 +522,8 @@ cudaError_t launch_part(const ClassLaunch& cl, const EriArgs& a, int mode, int p
         eri_grad_kernel<C><<<(unsigned)blocks, kEriThreads, 0, s>>>(cl, a);
         return cudaGetLastError();
       } else {
-        return launch_grad_fd<C>(cl, a, s);
+        if constexpr (C::L <= kGradAdMaxL) return launch_grad_ad<C>(cl, a, s);
+        else return launch_grad_fd<C>(cl, a, s);
       }
     }
     if (mode == MODE_SCHWARZ) {

@@ -431,6 +431,7 @@ def quartet_classes(lmax):
 
 
 GRAD_LMAX = 1  # gradient recurrences are generated for classes with every l <= GRAD_LMAX
+AD_LMAX = 7  # classes above take the finite-difference gradient kernel (compile time of the dual-number form)
 SPLIT_L = 5  # classes with la+lb+lc+ld >= SPLIT_L compile in four units each
 
 
@@ -522,8 +523,19 @@ def main(outdir, lmax):
                             '#include "../eri_kernel.cuh"\n' % (la, lb, lc, ld))
                     f.write("namespace fockgb {\ntemplate cudaError_t launch_part<%s, %d>%s;\n}  // namespace fockgb\n"
                             % (name, part, sig))
-        if max(la, lb, lc, ld) > GRAD_LMAX:
-            # finite-difference gradient kernel of the class, in a unit of its own
+        if max(la, lb, lc, ld) > GRAD_LMAX and la + lb + lc + ld <= AD_LMAX:
+            # gradient kernel of the class by dual-number differentiation of its
+            # recurrences (eri_grad_ad.cuh), in a unit of its own
+            with open(os.path.join(outdir, "inst_ad_%d%d%d%d.cu" % (la, lb, lc, ld)), "w") as f:
+                f.write('// Generated by gen_eri.py. Do not edit.\n#include "cls_%d%d%d%d.cuh"\n'
+                        '#include "../eri_grad_ad.cuh"\n' % (la, lb, lc, ld))
+                f.write("namespace fockgb {\n")
+                f.write("template cudaError_t launch_grad_ad<%s>(const ClassLaunch&, const EriArgs&, cudaStream_t);\n"
+                        % name)
+                f.write("}  // namespace fockgb\n")
+        elif max(la, lb, lc, ld) > GRAD_LMAX:
+            # (dd|dd): the dual-number form compiles for 5-8 minutes; the
+            # fourth-order finite difference of the class's integrals instead
             with open(os.path.join(outdir, "inst_fd_%d%d%d%d.cu" % (la, lb, lc, ld)), "w") as f:
                 f.write('// Generated by gen_eri.py. Do not edit.\n#include "cls_%d%d%d%d.cuh"\n'
                         '#include "../eri_grad_fd.cuh"\n' % (la, lb, lc, ld))
@@ -551,6 +563,7 @@ def main(outdir, lmax):
         f.write("    default: *hrr = 0; *neri = 0; return 0;\n  }\n}\n")
         f.write("constexpr int kGeneratedLmax = %d;\n" % lmax)
         f.write("constexpr int kGeneratedGradLmax = %d;\n" % GRAD_LMAX)
+        f.write("constexpr int kGradAdLmax = %d;\n" % AD_LMAX)
         f.write("}  // namespace fockgb\n")
     with open(os.path.join(outdir, "roofline_model.json"), "w") as f:
         json.dump(model, f, indent=1, sort_keys=True)

@@ -1,5 +1,8 @@
-"""The pair-data updates of the finite-difference gradient kernel (csrc/eri_grad_fd.cuh)
-against primitive pairs recomputed from scratch at the displaced centre (no GPU).
+"""The pair data of the gradient kernels against primitive pairs recomputed from
+scratch (no GPU): the seeds of the dual-number kernel (csrc/eri_grad_ad.cuh,
+the derivatives of P, P - A, K and A - B along the pair's centres), and the
+displaced-pair updates of the finite-difference kernel of (dd|dd)
+(csrc/eri_grad_fd.cuh).
 
 For exponents alpha (centre A), beta (centre B), p = alpha + beta, mu = alpha beta / p:
 moving A by delta gives P' = P + (alpha/p) delta, P' - A' = PA - (beta/p) delta,
@@ -16,6 +19,43 @@ def pair(alpha, beta, A, B, c=0.7):
     K = c * np.exp(-alpha * beta / p * AB.dot(AB)) / p
     P = (alpha * A + beta * B) / p
     return K, P, P - A, AB
+
+
+@pytest.mark.parametrize("seed", range(5))
+@pytest.mark.parametrize("which", ["A", "B"])
+def test_dual_number_seeds(seed, which):
+    """dP/dX, d(P - A)/dX, dK/dX, d(A - B)/dX of the seeds against complex-step derivatives."""
+    rng = np.random.default_rng(seed + 10)
+    alpha, beta = rng.uniform(0.05, 50.0, size=2)
+    A, B = rng.normal(size=3) * 2, rng.normal(size=3) * 2
+    K, P, PA, AB = pair(alpha, beta, A, B)
+    p = alpha + beta
+    mu = alpha * beta / p
+    h = 1e-30
+    for j in range(3):
+        d = np.zeros(3, dtype=complex)
+        d[j] = 1j * h
+        if which == "A":
+            Kc, Pc, PAc, ABc = pair(alpha, beta, A + d, B.astype(complex))
+            seed_P, seed_PA, seed_K, seed_AB = alpha / p, -beta / p, -2 * mu * AB[j] * K, 1.0
+        else:
+            Kc, Pc, PAc, ABc = pair(alpha, beta, A.astype(complex), B + d)
+            seed_P, seed_PA, seed_K, seed_AB = beta / p, beta / p, 2 * mu * AB[j] * K, -1.0
+        e = np.zeros(3)
+        e[j] = 1.0
+        assert np.allclose(Pc.imag / h, seed_P * e, rtol=0, atol=1e-14)
+        assert np.allclose(PAc.imag / h, seed_PA * e, rtol=0, atol=1e-14)
+        assert np.allclose(ABc.imag / h, seed_AB * e, rtol=0, atol=1e-14)
+        assert abs(Kc.imag / h - seed_K) <= 1e-13 * max(abs(seed_K), abs(K))
+
+
+def test_boys_derivative_relation(oracle_lib):
+    """dF_m/dT = -F_{m+1}, the Boys seed of the dual-number kernel (oracle's exact Boys)."""
+    for T in (1e-3, 0.5, 3.0, 17.0, 40.0):
+        for m in range(10):
+            h = 1e-5 * max(1.0, T)
+            fd = (oracle_lib.boys(T + h, m, oracle_lib.EXACT) - oracle_lib.boys(T - h, m, oracle_lib.EXACT)) / (2 * h)
+            assert abs(fd + oracle_lib.boys(T, m + 1, oracle_lib.EXACT)) < 1e-8 * max(1e-3, abs(fd))
 
 
 @pytest.mark.parametrize("seed", range(5))

@@ -61,7 +61,15 @@ def test_batch_mixed_scf_within_1e6(gpu_lib, clusters):
     with FockBatch(clusters, **SCF) as b:
         rc, r64 = b.scf()
     with FockBatch(clusters, precision=L.FOCK_PREC_MIXED, **SCF) as b:
-        rc2, rmx = b.scf()
+        rc2, rmx, dens = b.scf(densities=True)
+        # the FP32 share of a mixed build at the converged densities (the work
+        # counters describe the last build; the SCF itself ends in FP64)
+        import torch
+        D = torch.zeros(b.total, dtype=torch.float64, device="cuda")
+        for off, n, Dm in zip(b.offsets, b.nbf, dens):
+            D[off:off + n * n] = torch.from_numpy(Dm.reshape(-1))
+        G = torch.zeros_like(D)
+        b.build_jk_device(D.data_ptr(), G.data_ptr())
         st = b.stats()
     assert rc == 0 and rc2 == 0
     assert st["shell_quartets_fp32"] > 0
