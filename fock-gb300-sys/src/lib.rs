@@ -169,6 +169,7 @@ extern "C" {
     pub fn fock_nbasis(ctx: *const fock_ctx) -> c_int;
     pub fn fock_set_precision(ctx: *mut fock_ctx, precision: c_int, mixed_threshold: c_double) -> c_int;
     pub fn fock_eri_tensor(ctx: *mut fock_ctx, out_n4: *mut c_double) -> c_int;
+    pub fn fock_eri_list(ctx: *mut fock_ctx, nq: c_longlong, quartets: *const c_int, out: *mut c_double) -> c_int;
     pub fn fock_build_jk(ctx: *mut fock_ctx, D: *const c_double, G: *mut c_double) -> c_int;
     pub fn fock_build_jk_device(ctx: *mut fock_ctx, D_dev: *const c_double, G_dev: *mut c_double) -> c_int;
     pub fn fock_build_jk_noalloc(ctx: *mut fock_ctx, D_dev: *const c_double, G_dev: *mut c_double) -> c_int;

@@ -101,6 +101,15 @@ impl Context {
         Ok(ElectronTensor { data, size: self.n })
     }
 
+    /// BasisFunction::electron_repulsion_int (basis/src/lib.rs:41) for many
+    /// function quartets (i, j, k, l) at once.
+    pub fn electron_repulsion_ints(&mut self, quartets: &[[i32; 4]]) -> Result<Vec<f64>, Error> {
+        let flat: Vec<i32> = quartets.iter().flat_map(|q| q.iter().copied()).collect();
+        let mut out = vec![0.0; quartets.len()];
+        check(unsafe { fock_eri_list(self.raw, quartets.len() as i64, flat.as_ptr(), out.as_mut_ptr()) })?;
+        Ok(out)
+    }
+
     /// G = J - K/2 of a symmetric density (the Fock build of scf/src/lib.rs:177-187).
     pub fn build_jk(&mut self, d: &[f64]) -> Result<Vec<f64>, Error> {
         if d.len() != self.n * self.n {

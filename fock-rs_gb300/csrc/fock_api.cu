@@ -5,6 +5,7 @@
 //                     class-sorted quartet plans (device lists)
 //   fock_build_jk     fused ERI + J/K on the device (eri_kernel.cuh)
 //   fock_eri_tensor   full N^4 tensor (debug / parity)
+//   fock_eri_list     (ij|kl) of listed function quartets
 //   fock_scf          RHF with device-resident FP64 linear algebra
 //
 // Reference interfaces replaced: ElectronTensor::from_basis
@@ -1381,6 +1382,37 @@ int fock_eri_tensor(fock_ctx* c, double* out) {
   return FOCK_OK;
 }
 
+int fock_eri_list(fock_ctx* c, long long nq, const int* quartets, double* out) {
+  if (!c || nq < 0 || (nq > 0 && (!quartets || !out)) || c->nmol != 1) return FOCK_ERR_INVALID_ARG;
+  if (nq == 0) return FOCK_OK;
+  const int n = c->nbf;
+  for (long long t = 0; t < 4 * nq; ++t)
+    if (quartets[t] < 0 || quartets[t] >= n) return FOCK_ERR_INVALID_ARG;
+  CK(cudaSetDevice(c->device));
+  int* d_q = nullptr;
+  double* d_out = nullptr;
+  cudaError_t e = cudaMalloc(&d_q, (size_t)nq * 4 * sizeof(int));
+  if (e == cudaSuccess) e = dalloc(&d_out, (size_t)nq);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_q, quartets, (size_t)nq * 4 * sizeof(int), cudaMemcpyHostToDevice, c->stream);
+  const int flags = c->opt.eri_mode == FOCK_ERI_REFCOMPAT ? (MD_BOYS_LUT | MD_X_DEFECT) : 0;
+  if (e == cudaSuccess) {
+    e = md_eri_list(md_basis(c), md_tables(c), flags, d_q, nq, d_out, c->stream);
+    c->launches++;
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d_out, (size_t)nq * 8, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_q);
+  cudaFree(d_out);
+  CK(e);
+  if (c->opt.sign_convention == FOCK_SIGN_REFERENCE)
+    for (long long t = 0; t < nq; ++t) {
+      const int* q = quartets + 4 * t;
+      out[t] *= c->fsign[q[0]] * c->fsign[q[1]] * c->fsign[q[2]] * c->fsign[q[3]];
+    }
+  return FOCK_OK;
+}
+
 int fock_one_electron(fock_ctx* c, double* S, double* T, double* V) {
   if (!c || !S || !T || !V) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
@@ -1684,7 +1716,10 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
           CUSOLVER_STATUS_SUCCESS) { cleanup(); return FOCK_ERR_CUDA; }
   double* work = small_eig ? mk(eig_small_work_elems((long long)nn, n, 1)) : mk(lwork);
   double* emeta = mk(4);  // eig_small's one-block layout: off, woff (long long), n, list (int)
-  if (!work || !emeta) { cleanup(); return FOCK_ERR_OOM; }
+  // eigenvectors of the orthogonalised Fock matrix (C' of C = X C'): each
+  // eigensolve of the loop starts from the previous one's
+  double* Cp = mk(nn);
+  if (!work || !emeta || !Cp) { cleanup(); return FOCK_ERR_OOM; }
   long long* e_off = reinterpret_cast<long long*>(emeta);
   int* e_n = reinterpret_cast<int*>(emeta + 2);
   if (small_eig) {
@@ -1692,6 +1727,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     const int im[2] = {n, 0};
     cku_init(cudaMemcpyAsync(e_off, lm, sizeof(lm), cudaMemcpyHostToDevice, c->stream));
     cku_init(cudaMemcpyAsync(e_n, im, sizeof(im), cudaMemcpyHostToDevice, c->stream));
+    cku_init(eye_blocks(Cp, e_off, e_n, e_n + 1, 1, n, c->stream));
   }
   int fail = init_ok ? FOCK_OK : FOCK_ERR_CUDA;
   auto cku = [&](cudaError_t x) { if (x != cudaSuccess && fail == FOCK_OK) fail = map_cuda(x); };
@@ -1720,11 +1756,13 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       }
     }
   }
-  // eigenvalues into w, eigenvectors of the symmetric Ain into Vout (Ain kept)
-  auto eig = [&](const double* Ain, double* Vout) {
+  // eigenvalues into w, eigenvectors of the symmetric Ain into Vout (Ain kept);
+  // warm: start from the vectors in Vout
+  auto eig = [&](const double* Ain, double* Vout, bool warm) {
     if (small_eig) {
-      cku(eig_small(Ain, Vout, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, s));
-      c->launches += eig_small_launches();
+      cku(eig_small(Ain, Vout, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, s,
+                    warm ? Vout : nullptr));
+      c->launches += eig_small_launches(warm);
     } else {
       cku(cudaMemcpyAsync(Vout, Ain, nn * 8, cudaMemcpyDeviceToDevice, s));
       cks(cusolverDnDsyevd(c->solver, CUSOLVER_EIG_MODE_VECTOR, CUBLAS_FILL_MODE_LOWER, n, Vout, n, w, work, lwork,
@@ -1733,7 +1771,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     }
   };
   // Loewdin X = U diag(w^-1/2) U^T (scf/src/lib.rs:139-146)
-  eig(S, U);
+  eig(S, U, false);
   cku(k_scale_cols(U, w, W, n, s));
   c->launches++;
   gemm(CUBLAS_OP_N, CUBLAS_OP_T, n, &one, W, U, X);
@@ -1741,8 +1779,8 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   auto density_from = [&](const double* Fin, double* Dout) {
     gemm(CUBLAS_OP_T, CUBLAS_OP_N, n, &one, X, Fin, T1);  // X^T F
     gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, T1, X, T2);   // X^T F X
-    eig(T2, T1);                                          // C' in T1
-    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, X, T1, C);    // C = X C'
+    eig(T2, Cp, true);                                    // C'
+    gemm(CUBLAS_OP_N, CUBLAS_OP_N, n, &one, X, Cp, C);    // C = X C'
     if (nocc > 0) {
       ckb(cublasDgemm(c->blas, CUBLAS_OP_N, CUBLAS_OP_T, n, n, nocc, &two, C, n, C, n, &zero, Dout, n));
       c->launches++;
@@ -1822,7 +1860,10 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
   // host waits once per phase instead of once per iteration.  The decisions
   // are the host loop's below, in the same order.
   bool graph_done = false;
-  if (small_eig && !refc && c->opt.max_iters >= 0 && fail == FOCK_OK) {
+  // FOCK_GB300_SCF_HOST_LOOP=1: the host-driven loop below instead (same
+  // kernels, one launch at a time, so that profilers list them)
+  const bool host_loop = std::getenv("FOCK_GB300_SCF_HOST_LOOP") != nullptr;
+  if (small_eig && !refc && c->opt.max_iters >= 0 && !host_loop && fail == FOCK_OK) {
     double* Ecur = mk(nn);
     ScfDevState* dst = reinterpret_cast<ScfDevState*>(mk((sizeof(ScfDevState) + 7) / 8));
     if (!Ecur || !dst) { cleanup(); return FOCK_ERR_OOM; }
@@ -1871,8 +1912,9 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       if (e == cudaSuccess) {
         int kn = 0;
         auto ck = [&](cudaError_t x) { if (e == cudaSuccess) e = x; };
-        auto gm = [&](bool ta, bool tb, double alpha, int kd, const double* A, const double* B, double* Cc) {
-          ck(gemm_blocks(ta, tb, alpha, kd, A, B, Cc, e_off, e_n, e_n + 1, 1, n, cs));
+        auto gm = [&](bool ta, bool tb, double alpha, int kd, const double* A, const double* B, double* Cc,
+                      bool sym = false) {
+          ck(gemm_blocks(ta, tb, alpha, kd, A, B, Cc, e_off, e_n, e_n + 1, 1, n, cs, sym));
           kn++;
         };
         ck(ks_iter_begin(dst, cs));
@@ -1893,17 +1935,17 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
         const double* Fuse = Fd;
         if (c->opt.level_shift != 0.0) {  // F + b (S - 1/2 S D S)
           gm(false, false, 1.0, -1, S, Dg, T1);
-          gm(false, false, 1.0, -1, T1, S, T2);
+          gm(false, false, 1.0, -1, T1, S, T2, true);          // S D S
           ck(ks_level_shift(Fd, S, T2, dst, (long long)nn, Fsh, cs));
           kn++;
           Fuse = Fsh;
         }
         gm(true, false, 1.0, -1, X, Fuse, T1);                 // X^T F
-        gm(false, false, 1.0, -1, T1, X, T2);                  // X^T F X
-        ck(eig_small(T2, T1, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, cs));
-        kn += eig_small_launches();
-        gm(false, false, 1.0, -1, X, T1, C);                   // C = X C'
-        if (nocc > 0) gm(false, true, 2.0, nocc, C, C, Dn);    // D = 2 C_occ C_occ^T
+        gm(false, false, 1.0, -1, T1, X, T2, true);            // X^T F X
+        ck(eig_small(T2, Cp, w, e_off, e_off + 1, e_n, e_n + 1, 1, n, work, (long long)nn, n, cs, Cp));
+        kn += eig_small_launches(true);
+        gm(false, false, 1.0, -1, X, Cp, C);                   // C = X C'
+        if (nocc > 0) gm(false, true, 2.0, nocc, C, C, Dn, true);  // D = 2 C_occ C_occ^T
         else ck(cudaMemsetAsync(Dn, 0, nn * 8, cs));
         ck(k_energy(Dn, H, Gg, (int)nn, scal + 1, cs));        // reference energy: new D, old G
         ck(ks_control(dst, scal, h, cs));
@@ -2205,6 +2247,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   double *X = (double*)mk(TB), *W = (double*)mk(TB), *U = (double*)mk(TB), *w = (double*)mk(woff[nmol] * 8);
   double *F = (double*)mk(TB), *Fd = (double*)mk(TB), *G = (double*)mk(TB), *Dm = (double*)mk(TB);
   double *Dn = (double*)mk(TB), *Cm = (double*)mk(TB), *T1 = (double*)mk(TB), *T2 = (double*)mk(TB);
+  double* Cw = (double*)mk(TB);  // C' per molecule (C = X C')
   double *Fring = (double*)mk(TB * ring), *Ering = (double*)mk(TB * ring);
   const double shift = c->opt.level_shift;
   double* Fsh = shift != 0.0 ? (double*)mk(TB) : F;
@@ -2280,12 +2323,13 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   if (!ok) { if (sp) cusolverDnDestroyParams(sp); cleanup(); return FOCK_ERR_OOM; }
   const bool trace_syev = std::getenv("FOCK_GB300_TRACE") != nullptr;
   int syev_calls = 0;
-  // eigenvalues into w, eigenvectors of the symmetric blocks of Ain into Vout (Ain kept)
-  auto eig = [&](const double* Ain, double* Vout) {
+  // eigenvalues into w, eigenvectors of the symmetric blocks of Ain into Vout
+  // (Ain kept); warm: start from the vectors in Vout
+  auto eig = [&](const double* Ain, double* Vout, bool warm) {
     if (n_elist > 0) {
       cku(eig_small(Ain, Vout, w, c->d_mol_off, d_woff, c->d_mol_n, d_elist, n_elist, nmax_small, ework, T,
-                    woff[nmol], s));
-      c->launches += eig_small_launches();
+                    woff[nmol], s, warm ? Vout : nullptr));
+      c->launches += eig_small_launches(warm);
     }
     for (const Run& r : act) {
       if (r.n <= kEigMaxN) continue;
@@ -2309,15 +2353,19 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   };
   // Loewdin X = U diag(w^-1/2) U^T
   upload_elist();
-  eig(S, U);
+  eig(S, U, false);
+  if (n_elist > 0) {  // C' of every molecule, each eigensolve starting from the previous one's
+    cku(eye_blocks(Cw, c->d_mol_off, c->d_mol_n, d_elist, n_elist, nmax_small, s));
+    c->launches++;
+  }
   cku(kb_scale_cols(U, w, d_woff, c->d_mol_off, c->d_mol_n, nmol, T, W, s));
   c->launches++;
   for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.n, &one, W, U, X);
   auto density_from = [&](const double* Fin, double* Dout) {
     for (const Run& r : act) gemm(r, CUBLAS_OP_T, CUBLAS_OP_N, r.n, &one, X, Fin, T1);
     for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, T1, X, T2);
-    eig(T2, T1);
-    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, T1, Cm);
+    eig(T2, Cw, true);
+    for (const Run& r : act) gemm(r, CUBLAS_OP_N, CUBLAS_OP_N, r.n, &one, X, Cw, Cm);
     for (const Run& r : act) {
       if (r.nocc > 0) {
         gemm(r, CUBLAS_OP_N, CUBLAS_OP_T, r.nocc, &two, Cm, Cm, Dout);

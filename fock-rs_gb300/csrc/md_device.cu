@@ -439,6 +439,17 @@ __global__ void md_tensor_kernel(const MdBasis B, const MdTables tb, int flags, 
   out[((I * n + J) * n + K) * n + Lq] = v;
 }
 
+// (ij|kl) of listed function quartets q[4t .. 4t+3], one thread each: the
+// per-function integral of BasisFunction::electron_repulsion_int
+// (basis/src/lib.rs:41, contracted_gaussian.rs), with no zeroing of small
+// values (that belongs to ElectronTensor::from_basis).
+__global__ void md_eri_list_kernel(const MdBasis B, const MdTables tb, int flags, const int* __restrict__ q,
+                                   long long nq, double* __restrict__ out) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= nq) return;
+  out[t] = md_eri_contracted(B, tb, q[4 * t], q[4 * t + 1], q[4 * t + 2], q[4 * t + 3], flags);
+}
+
 // G = J - K/2 from the full tensor, as scf/src/lib.rs:167-187:
 // G_ij = sum_xy D_xy ((ij|xy) - 1/2 (ix|jy)).  One thread per (i, j).
 __global__ void g_from_tensor_kernel(const double* __restrict__ eri, const double* __restrict__ D, int n, double* G) {
@@ -477,6 +488,14 @@ cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, doubl
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+cudaError_t md_eri_list(const MdBasis& B, const MdTables& tb, int flags, const int* q, long long nq, double* out,
+                        cudaStream_t s) {
+  if (nq <= 0) return cudaSuccess;
+  const int thr = 64;
+  md_eri_list_kernel<<<(unsigned)((nq + thr - 1) / thr), thr, 0, s>>>(B, tb, flags, q, nq, out);
+  return cudaGetLastError();
 }
 
 // Molecular orbital on a cubic grid (volumetric/src/main.rs:100-125,

@@ -32,6 +32,10 @@ cudaError_t md_one_electron(const MdBasis& B, const MdTables& tb, const double* 
                             double* S, double* T, double* V, cudaStream_t s);
 cudaError_t md_eri_tensor(const MdBasis& B, const MdTables& tb, int flags, double screen, double* diag, double* out,
                           cudaStream_t s);
+// (ij|kl) for nq listed function quartets q (4 ints each, device), textbook
+// convention, no screening.
+cudaError_t md_eri_list(const MdBasis& B, const MdTables& tb, int flags, const int* q, long long nq, double* out,
+                        cudaStream_t s);
 cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const double* atoms, int natom,
                                  const int* func_atom, int flags, const double* D, const double* W, double* grad,
                                  cudaStream_t s);

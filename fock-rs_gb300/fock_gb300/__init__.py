@@ -8,6 +8,9 @@ reads the same:
   * ``try_scf(atoms, max_iters, epsilon, molecule_charge)`` -> HartreeFockResult
     or None                                  scf/src/lib.rs:61-66, 27-37
   * ``FockBuilder(atoms).build(D)`` = G = J - K/2 of scf/src/lib.rs:177-187
+  * ``electron_repulsion_int(atoms, a, b, c, d)``  basis/src/lib.rs:41 (one
+    integral over four basis functions; ``FockContext.electron_repulsion_ints``
+    takes many quartets at once)
 
 Every call goes through the C ABI (libfock_gb300.so) to the sm_103a kernels.
 """
@@ -87,6 +90,14 @@ class FockContext:
     def eri_tensor(self) -> np.ndarray:
         out = np.zeros(self.n ** 4)
         check(lib().fock_eri_tensor(self.handle, _dp(out)), "fock_eri_tensor")
+        return out
+
+    def electron_repulsion_ints(self, quartets) -> np.ndarray:
+        """(ij|kl) for rows (i, j, k, l) of function indices (fock_eri_list)."""
+        q = np.ascontiguousarray(np.asarray(quartets, dtype=np.int32).reshape(-1, 4))
+        out = np.zeros(len(q))
+        check(lib().fock_eri_list(self.handle, len(q), q.ctypes.data_as(C.POINTER(C.c_int)), _dp(out)),
+              "fock_eri_list")
         return out
 
     def build_jk(self, D) -> np.ndarray:
@@ -289,6 +300,14 @@ class HartreeFockResult:
     scf_seconds: float = 0.0
     fock_seconds: float = 0.0
     fock_builds: int = 0
+
+
+def electron_repulsion_int(atoms: Sequence[Atom], a: int, b: int, c: int, d: int, **kw) -> float:
+    """BasisFunction::electron_repulsion_int (basis/src/lib.rs:41): (ab|cd)
+    over the functions a, b, c, d of the basis built on ``atoms`` (indices in
+    the reference's function order)."""
+    with FockContext(atoms, **kw) as ctx:
+        return float(ctx.electron_repulsion_ints([(a, b, c, d)])[0])
 
 
 def try_scf(atoms: Sequence[Atom], max_iters: int, epsilon: float, molecule_charge: int = 0,

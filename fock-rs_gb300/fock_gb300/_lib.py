@@ -97,6 +97,7 @@ def lib():
         L.fock_nbasis.argtypes = [vp]
         L.fock_set_precision.argtypes = [vp, C.c_int, C.c_double]
         L.fock_eri_tensor.argtypes = [vp, dp]
+        L.fock_eri_list.argtypes = [vp, C.c_longlong, C.POINTER(C.c_int), dp]
         L.fock_build_jk.argtypes = [vp, dp, dp]
         L.fock_build_jk_device.argtypes = [vp, vp, vp]
         L.fock_build_jk_noalloc.argtypes = [vp, vp, vp]

@@ -155,6 +155,15 @@ int fock_set_precision(fock_ctx* ctx, int precision, double mixed_threshold);
  * per-integral error of the mixed path; no density weighting here). */
 int fock_eri_tensor(fock_ctx* ctx, double* out_n4);
 
+/* Contracted integrals (ij|kl) of nq listed function quartets: quartets[4q ..
+ * 4q+3] = (i, j, k, l), function indices of a single-molecule context; out[q]
+ * receives (ij|kl) in the context's eri_mode and sign convention, with no
+ * zeroing of small values.  Replaces BasisFunction::electron_repulsion_int
+ * (basis/src/lib.rs:41; contracted_gaussian.rs electron_repulsion_int), the
+ * reference's one-integral entry: one GPU thread per quartet, each a
+ * per-function McMurchie-Davidson sum like the reference's. */
+int fock_eri_list(fock_ctx* ctx, long long nq, const int* quartets, double* out);
+
 /* G = J - K/2 for a symmetric density D (host arrays), the two-electron part
  * of F = H + G (scf/src/lib.rs:177-187), integral-direct: no N^4 storage. */
 int fock_build_jk(fock_ctx* ctx, const double* D, double* G);

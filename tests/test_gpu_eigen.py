@@ -4,8 +4,14 @@ numpy's LAPACK eigh on symmetric matrices of the SCF's shapes: random spectra,
 exactly degenerate and tightly clustered eigenvalues (symmetric molecules), an
 overlap-like matrix with small eigenvalues (Loewdin) and real Fock matrices.
 
-Tolerances: eigenvalues and the residual ||A V - V diag(w)|| 1e-12 * ||A||;
-orthogonality ||V^T V - I|| 1e-11."""
+Tolerances: eigenvalues and the residual ||A V - V diag(w)|| 1e-13 * ||A||;
+orthogonality ||V^T V - I|| 1e-13 (the refinement stops at the FP64 rounding
+level, ~1e-15).  The SCF's orbitals must be S-orthonormal and its density
+idempotent: an error of 1e-9 there moves the SCF energy at first order and
+shows as 3e-5 Eh/bohr in finite-difference gradients.  Their bound, 2e-11, is
+set by the Loewdin X = S^-1/2 (smallest overlap eigenvalue 6.7e-4 for
+benzene/6-31G: rounding of S alone gives X^T S X - I ~ 1e-13, numpy's own X
+included, and C^T S C - I ~ 5e-12)."""
 import ctypes as C
 
 import numpy as np
@@ -30,7 +36,7 @@ def sorted_eigs(lib, A):
     return w, V
 
 
-def check(lib, A, tol=1e-12, orth=1e-11):
+def check(lib, A, tol=1e-13, orth=1e-13):
     w, V = sorted_eigs(lib, A)
     ref = np.linalg.eigvalsh(A)
     scale = max(1.0, np.abs(ref).max())
@@ -71,12 +77,19 @@ def test_overlap_like_small_eigenvalues(gpu_lib):
                               4))
 
 
-@pytest.mark.parametrize("name", ["benzene", "water_cluster"])
-def test_fock_and_overlap_matrices(gpu_lib, name):
+def scf_atoms(name):
     if name == "benzene":
-        atoms = B.build_atoms("6-31G", *M.benzene())  # D6h: many degenerate orbitals
-    else:
-        atoms = B.build_atoms("6-31G", *M.water_cluster(8, seed=3))
+        return B.build_atoms("6-31G", *M.benzene())  # D6h: many degenerate orbitals
+    if name == "water_dimer":  # 6-31G*: an overlap eigenvalue pair 1e-9 apart
+        return B.build_atoms("6-31G*", *M.water_cluster(2, seed=0))
+    if name == "octane":  # n = 108
+        return B.build_atoms("6-31G", *M.octane(seed=0))
+    return B.build_atoms("6-31G", *M.water_cluster(8, seed=3))
+
+
+@pytest.mark.parametrize("name", ["benzene", "water_cluster", "water_dimer", "octane"])
+def test_fock_and_overlap_matrices(gpu_lib, name):
+    atoms = scf_atoms(name)
     with FockContext(atoms) as ctx:
         S, T, V = ctx.one_electron()
         rc, r, eps, D, Cm = ctx.scf(0)
@@ -89,6 +102,20 @@ def test_fock_and_overlap_matrices(gpu_lib, name):
     ws, Us = np.linalg.eigh(S)
     X = (Us / np.sqrt(ws)) @ Us.T
     check(gpu_lib, X.T @ F @ X)
+
+
+@pytest.mark.parametrize("name", ["benzene", "water_dimer", "octane"])
+def test_scf_orbitals_orthonormal(gpu_lib, name):
+    """C^T S C = I and D S D = 2 D for the SCF's result (warm-started
+    eigensolves inside the device-driven loop)."""
+    with FockContext(scf_atoms(name), epsilon=1e-10) as ctx:
+        S, T, V = ctx.one_electron()
+        rc, r, eps, D, Cm = ctx.scf(0)
+        assert rc == 0 and r.converged
+    n = S.shape[0]
+    assert np.abs(Cm.T @ S @ Cm - np.eye(n)).max() < 2e-11
+    assert np.abs(D @ S @ D - 2 * D).max() < 2e-11
+    assert np.all(np.diff(eps) >= 0)
 
 
 def test_sorted_eigs_rejects_bad_input(gpu_lib):
