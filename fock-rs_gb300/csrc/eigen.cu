@@ -59,8 +59,11 @@ constexpr int kFinishWarps = 8;
 // Refinement steps at most: every test spectrum (random, degenerate,
 // clustered, overlap-like, Fock and overlap matrices of the SCF) stops after
 // two to four updates; the bound only matters for matrices that never reach
-// the rounding level.
-constexpr int kRefineMax = 6;
+// the rounding level.  The FP32 Jacobi stops at off-diagonals of 1e-5 of the
+// largest diagonal entry: a further sweep costs more than the refinement step
+// it saves.
+constexpr float kJacobiTol = 1e-5f;
+constexpr int kRefineMax = 7;
 constexpr double kClusterRel = 1e-5;
 // stop when the residuals are below kConvC sqrt(n) u (relative to ||A|| for S)
 constexpr double kConvC = 4.0;
@@ -589,11 +592,11 @@ cudaError_t eig_small(const double* A, double* Vout, double* wout, const long lo
                               kGateNone, 0);
     launch_gemm<true, false>(gs1, s, Vwarm, AX, Sm, nullptr, nullptr, nullptr, 1.0, -1, off, nsz, list, nullptr,
                              kGateNone, 1);
-    jacobi32_kernel<<<nlist, kJacThreads, smem, s>>>(Sm, X1, off, nsz, list, 20, 2e-6f, flags);
+    jacobi32_kernel<<<nlist, kJacThreads, smem, s>>>(Sm, X1, off, nsz, list, 20, kJacobiTol, flags);
     launch_gemm<false, false>(g1, s, Vwarm, X1, X0, nullptr, nullptr, nullptr, 1.0, -1, off, nsz, list, flags,
                               kGateCopyIdent, 0);
   } else {
-    jacobi32_kernel<<<nlist, kJacThreads, smem, s>>>(A, X0, off, nsz, list, 20, 2e-6f, flags);
+    jacobi32_kernel<<<nlist, kJacThreads, smem, s>>>(A, X0, off, nsz, list, 20, kJacobiTol, flags);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   const dim3 gu((nmax + kTile - 1) / kTile, nlist, 1);

@@ -292,47 +292,61 @@ cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const dou
   return cudaGetLastError();
 }
 
-// S, T, V for function pairs i <= j; one thread per pair.
+// S, T, V for function pairs i <= j; one warp per pair.  The lanes take the
+// pair's (primitive pair, nucleus) items of V and its primitive pairs of S and
+// T (a thread per pair left most of the GPU idle: 2,211 pairs for benzene),
+// then reduce in a fixed order.
 __global__ void one_electron_kernel(const MdBasis B, const MdTables tb, const double* __restrict__ atoms /*x,y,z,Z*/,
                                     int natom, int flags, double* S, double* T, double* V) {
   const int n = B.nfunc;
   const long long npair = (long long)n * (n + 1) / 2;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= npair) return;
+  const long long t = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (t >= npair) return;  // whole warps
   int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
   while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
   while ((long long)i * (i + 1) / 2 > t) --i;
   const int j = (int)(t - (long long)i * (i + 1) / 2);
   const MdFunc fa = B.funcs[j], fb = B.funcs[i];  // j <= i
   const double diff[3] = {fb.c[0] - fa.c[0], fb.c[1] - fa.c[1], fb.c[2] - fa.c[2]};
+  const int L = fa.ang[0] + fa.ang[1] + fa.ang[2] + fb.ang[0] + fb.ang[1] + fb.ang[2];
+  const int nprim = fa.np * fb.np;
+  const int nitem = nprim * (natom + 1);  // nucleus index natom: overlap and kinetic
   double s = 0.0, k = 0.0, v = 0.0;
-  for (int pa = 0; pa < fa.np; ++pa)
-    for (int pb = 0; pb < fb.np; ++pb) {
-      const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
-      const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb];
+  for (int it = lane; it < nitem; it += 32) {
+    const int pp = it % nprim, c = it / nprim;
+    const int pa = pp / fb.np, pb = pp - pa * fb.np;
+    const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
+    const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb];
+    if (c == natom) {
       s += cc * prim_overlap(fa.ang, a, fb.ang, b, diff);
       k += cc * prim_kinetic(fa.ang, a, fb.ang, b, diff);
-      // nuclear attraction: -Z 2pi/p sum E E E R(p, C - P)
-      const double p = a + b;
-      double P[3];
-      for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / p;
-      ETable<2, 2> E[3];
-      for (int x = 0; x < 3; ++x) etab_build(fa.ang[x], fb.ang[x], diff[x], a, b, E[x]);
-      const int L = fa.ang[0] + fa.ang[1] + fa.ang[2] + fb.ang[0] + fb.ang[1] + fb.ang[2];
-      for (int c = 0; c < natom; ++c) {
-        const double dcp[3] = {atoms[4 * c] - P[0], atoms[4 * c + 1] - P[1], atoms[4 * c + 2] - P[2]};
-        const double r2 = dcp[0] * dcp[0] + dcp[1] * dcp[1] + dcp[2] * dcp[2];
-        RTable<4> R;
-        rtab_build(L, p, dcp, r2, flags, tb, R);
-        double sum = 0.0;
-        for (int tt = 0; tt <= fa.ang[0] + fb.ang[0]; ++tt)
-          for (int u = 0; u <= fa.ang[1] + fb.ang[1]; ++u)
-            for (int w = 0; w <= fa.ang[2] + fb.ang[2]; ++w)
-              sum += E[0].e[fa.ang[0]][fb.ang[0]][tt] * E[1].e[fa.ang[1]][fb.ang[1]][u] *
-                     E[2].e[fa.ang[2]][fb.ang[2]][w] * R.at(tt, u, w);
-        v += cc * (-atoms[4 * c + 3] * (2.0 * M_PI) / p * sum);
-      }
+      continue;
     }
+    // nuclear attraction of nucleus c: -Z 2pi/p sum E E E R(p, C - P)
+    const double p = a + b;
+    double P[3];
+    for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / p;
+    ETable<2, 2> E[3];
+    for (int x = 0; x < 3; ++x) etab_build(fa.ang[x], fb.ang[x], diff[x], a, b, E[x]);
+    const double dcp[3] = {atoms[4 * c] - P[0], atoms[4 * c + 1] - P[1], atoms[4 * c + 2] - P[2]};
+    const double r2 = dcp[0] * dcp[0] + dcp[1] * dcp[1] + dcp[2] * dcp[2];
+    RTable<4> R;
+    rtab_build(L, p, dcp, r2, flags, tb, R);
+    double sum = 0.0;
+    for (int tt = 0; tt <= fa.ang[0] + fb.ang[0]; ++tt)
+      for (int u = 0; u <= fa.ang[1] + fb.ang[1]; ++u)
+        for (int w = 0; w <= fa.ang[2] + fb.ang[2]; ++w)
+          sum += E[0].e[fa.ang[0]][fb.ang[0]][tt] * E[1].e[fa.ang[1]][fb.ang[1]][u] *
+                 E[2].e[fa.ang[2]][fb.ang[2]][w] * R.at(tt, u, w);
+    v += cc * (-atoms[4 * c + 3] * (2.0 * M_PI) / p * sum);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s += __shfl_down_sync(0xffffffffu, s, o);
+    k += __shfl_down_sync(0xffffffffu, k, o);
+    v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  if (lane != 0) return;
   const double sg = fsign(fa) * fsign(fb);  // reference -> textbook convention
   s *= sg; k *= sg; v *= sg;
   S[(size_t)i * n + j] = s; S[(size_t)j * n + i] = s;
@@ -467,8 +481,8 @@ __global__ void g_from_tensor_kernel(const double* __restrict__ eri, const doubl
 cudaError_t md_one_electron(const MdBasis& B, const MdTables& tb, const double* atoms, int natom, int flags,
                             double* S, double* T, double* V, cudaStream_t s) {
   const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
-  const int thr = 64;
-  one_electron_kernel<<<(unsigned)((np + thr - 1) / thr), thr, 0, s>>>(B, tb, atoms, natom, flags, S, T, V);
+  const int thr = 128;  // four pairs (warps) per block
+  one_electron_kernel<<<(unsigned)((np * 32 + thr - 1) / thr), thr, 0, s>>>(B, tb, atoms, natom, flags, S, T, V);
   return cudaGetLastError();
 }
 

@@ -124,46 +124,69 @@ __global__ void diis_dots_kernel(const double* Ering, int nn, int slot, int used
 
 // Pulay DIIS: solve [B -1; -1 0] c = [0; -1] over the m slots listed in
 // order[0..m) (oldest first) by Gaussian elimination with partial pivoting
-// (the reference inverts the same matrix, scf/src/utils.rs:102-138).
-// coef[0..m) receives c; coef[m] = 1 on success, 0 if singular.
-__global__ void diis_solve_kernel(const double* B, int ring, const int* order, int m, double* coef) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double A[17 * 17], rhs[17];
+// (the reference inverts the same matrix, scf/src/utils.rs:102-138), one warp:
+// lane r owns row r, the pivot is the first largest |A_rc| (as a serial scan
+// picks it), back substitution by warp dot products.  A (17 x 17) and rhs (17)
+// are this warp's shared scratch.  c[0..m) into coef, coef[ok_at] = 1 on
+// success, 0 if singular.
+__device__ void diis_solve_warp(const double* __restrict__ B, int ring, const int* order, int m, double* coef,
+                                int ok_at, double* A, double* rhs) {
+  const int lane = threadIdx.x & 31;
   const int M = m + 1;
-  for (int i = 0; i < m; ++i) {
-    for (int j = 0; j < m; ++j) A[i * M + j] = B[order[i] * ring + order[j]];
-    A[i * M + m] = -1.0;
-    A[m * M + i] = -1.0;
-    rhs[i] = 0.0;
+  for (int e = lane; e < M * M; e += 32) {
+    const int i = e / M, j = e - (e / M) * M;
+    double x;
+    if (i < m && j < m) x = B[order[i] * ring + order[j]];
+    else if (i == m && j == m) x = 0.0;
+    else x = -1.0;
+    A[e] = x;
   }
-  A[m * M + m] = 0.0;
-  rhs[m] = -1.0;
+  if (lane < M) rhs[lane] = lane < m ? 0.0 : -1.0;
+  __syncwarp();
   bool ok = true;
-  for (int c = 0; c < M && ok; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < M; ++r)
-      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
-    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
+  for (int c = 0; c < M; ++c) {
+    double v = (lane >= c && lane < M) ? fabs(A[lane * M + c]) : -1.0;
+    int idx = lane;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double v2 = __shfl_xor_sync(0xffffffffu, v, o);
+      const int i2 = __shfl_xor_sync(0xffffffffu, idx, o);
+      if (v2 > v || (v2 == v && i2 < idx)) { v = v2; idx = i2; }
+    }
+    if (!(v > 1e-300)) { ok = false; break; }
+    const int piv = idx;
     if (piv != c) {
-      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
-      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
+      if (lane < M) {
+        const double t = A[c * M + lane];
+        A[c * M + lane] = A[piv * M + lane];
+        A[piv * M + lane] = t;
+      }
+      if (lane == 0) { const double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t; }
     }
-    for (int r = c + 1; r < M; ++r) {
-      const double f = A[r * M + c] / A[c * M + c];
-      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
-      rhs[r] -= f * rhs[c];
+    __syncwarp();
+    if (lane > c && lane < M) {
+      const double f = A[lane * M + c] / A[c * M + c];
+      for (int k = c; k < M; ++k) A[lane * M + k] -= f * A[c * M + k];
+      rhs[lane] -= f * rhs[c];
     }
+    __syncwarp();
   }
   if (ok) {
     for (int c = M - 1; c >= 0; --c) {
-      double s = rhs[c];
-      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
-      rhs[c] = s / A[c * M + c];
+      double d = (lane > c && lane < M) ? A[c * M + lane] * rhs[lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+      if (lane == 0) rhs[c] = (rhs[c] - d) / A[c * M + c];
+      __syncwarp();
       if (!isfinite(rhs[c])) ok = false;
     }
   }
-  for (int i = 0; i < m; ++i) coef[i] = ok ? rhs[i] : 0.0;
-  coef[m] = ok ? 1.0 : 0.0;
+  for (int i = lane; i < m; i += 32) coef[i] = ok ? rhs[i] : 0.0;
+  if (lane == 0) coef[ok_at] = ok ? 1.0 : 0.0;
+}
+
+// one warp: coef[m] = 1 on success
+__global__ void diis_solve_kernel(const double* B, int ring, const int* order, int m, double* coef) {
+  __shared__ double A[17 * 17], rhs[17];
+  diis_solve_warp(B, ring, order, m, coef, m, A, rhs);
 }
 
 // Fd = sum_i c_i F_{order[i]}; falls back to F_{last} when the solve failed.
@@ -377,50 +400,17 @@ __global__ void diis_dots_blocks_kernel(const double* Ering, long long total, in
   }
 }
 
-// Pulay DIIS per molecule (one thread each): solve [B -1; -1 0] c = [0; -1]
-// over the slots order[0..mu) by Gaussian elimination with partial pivoting.
-__global__ void diis_solve_blocks_kernel(const double* B, int ring, const int* order, int mu, double* coef,
-                                         int nmol) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= nmol) return;
-  const double* Bm = B + (long long)m * ring * ring;
-  double* cm = coef + (long long)m * (ring + 1);
-  double A[17 * 17], rhs[17];
-  const int M = mu + 1;
-  for (int i = 0; i < mu; ++i) {
-    for (int j = 0; j < mu; ++j) A[i * M + j] = Bm[order[i] * ring + order[j]];
-    A[i * M + mu] = -1.0;
-    A[mu * M + i] = -1.0;
-    rhs[i] = 0.0;
-  }
-  A[mu * M + mu] = 0.0;
-  rhs[mu] = -1.0;
-  bool ok = true;
-  for (int c = 0; c < M && ok; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < M; ++r)
-      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
-    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
-    if (piv != c) {
-      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
-      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
-    }
-    for (int r = c + 1; r < M; ++r) {
-      const double f = A[r * M + c] / A[c * M + c];
-      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
-      rhs[r] -= f * rhs[c];
-    }
-  }
-  if (ok) {
-    for (int c = M - 1; c >= 0; --c) {
-      double s = rhs[c];
-      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
-      rhs[c] = s / A[c * M + c];
-      if (!isfinite(rhs[c])) ok = false;
-    }
-  }
-  for (int i = 0; i < mu; ++i) cm[i] = ok ? rhs[i] : 0.0;
-  cm[ring] = ok ? 1.0 : 0.0;
+// Pulay DIIS per molecule, one warp each (diis_solve_warp).
+constexpr int kDiisWarps = 4;
+__global__ void __launch_bounds__(kDiisWarps * 32) diis_solve_blocks_kernel(const double* B, int ring,
+                                                                              const int* order, int mu,
+                                                                              double* coef, int nmol) {
+  __shared__ double A[kDiisWarps][17 * 17], rhs[kDiisWarps][17];
+  const int w = threadIdx.x >> 5;
+  const int m = blockIdx.x * kDiisWarps + w;
+  if (m >= nmol) return;  // whole warps
+  diis_solve_warp(B + (long long)m * ring * ring, ring, order, mu, coef + (long long)m * (ring + 1), ring, A[w],
+                  rhs[w]);
 }
 
 __global__ void diis_extrapolate_blocks_kernel(const double* Fring, long long total, const int* order, int mu,
@@ -478,7 +468,8 @@ cudaError_t kb_diis_dots(const double* Ering, long long total, int slot, int nus
 }
 cudaError_t kb_diis_solve(const double* B, int ring, const int* order, int mu, double* coef, int nmol,
                           cudaStream_t s) {
-  diis_solve_blocks_kernel<<<nblk(nmol, 32), 32, 0, s>>>(B, ring, order, mu, coef, nmol);
+  diis_solve_blocks_kernel<<<(nmol + kDiisWarps - 1) / kDiisWarps, kDiisWarps * 32, 0, s>>>(B, ring, order, mu,
+                                                                                            coef, nmol);
   return cudaGetLastError();
 }
 cudaError_t kb_diis_extrapolate(const double* Fring, long long total, const int* order, int mu, const double* coef,
@@ -554,45 +545,13 @@ __global__ void diis_dots_st_kernel(const double* Ering, int nn, const ScfDevSta
 // as diis_solve_kernel over the state's slots; coef[ring] = 1 when the
 // extrapolation applies (enough vectors and a regular system), 0 otherwise
 __global__ void diis_solve_st_kernel(const double* B, int ring, const ScfDevState* st, double* coef) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  __shared__ double A[17 * 17], rhs[17];
   const int m = st->nused;
-  if (m < st->diis_start) { coef[ring] = 0.0; return; }
-  double A[17 * 17], rhs[17];
-  const int M = m + 1;
-  for (int i = 0; i < m; ++i) {
-    for (int j = 0; j < m; ++j) A[i * M + j] = B[st->order[i] * ring + st->order[j]];
-    A[i * M + m] = -1.0;
-    A[m * M + i] = -1.0;
-    rhs[i] = 0.0;
+  if (m < st->diis_start) {
+    if (threadIdx.x == 0) coef[ring] = 0.0;
+    return;
   }
-  A[m * M + m] = 0.0;
-  rhs[m] = -1.0;
-  bool ok = true;
-  for (int c = 0; c < M && ok; ++c) {
-    int piv = c;
-    for (int r = c + 1; r < M; ++r)
-      if (fabs(A[r * M + c]) > fabs(A[piv * M + c])) piv = r;
-    if (!(fabs(A[piv * M + c]) > 1e-300)) { ok = false; break; }
-    if (piv != c) {
-      for (int k = 0; k < M; ++k) { double t = A[c * M + k]; A[c * M + k] = A[piv * M + k]; A[piv * M + k] = t; }
-      double t = rhs[c]; rhs[c] = rhs[piv]; rhs[piv] = t;
-    }
-    for (int r = c + 1; r < M; ++r) {
-      const double f = A[r * M + c] / A[c * M + c];
-      for (int k = c; k < M; ++k) A[r * M + k] -= f * A[c * M + k];
-      rhs[r] -= f * rhs[c];
-    }
-  }
-  if (ok) {
-    for (int c = M - 1; c >= 0; --c) {
-      double s = rhs[c];
-      for (int k = c + 1; k < M; ++k) s -= A[c * M + k] * rhs[k];
-      rhs[c] = s / A[c * M + c];
-      if (!isfinite(rhs[c])) ok = false;
-    }
-  }
-  for (int i = 0; i < m; ++i) coef[i] = ok ? rhs[i] : 0.0;
-  coef[ring] = ok ? 1.0 : 0.0;
+  diis_solve_warp(B, ring, st->order, m, coef, ring, A, rhs);
 }
 
 __global__ void diis_extrapolate_st_kernel(const double* Fring, int nn, const ScfDevState* st, const double* coef,
