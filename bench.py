@@ -38,7 +38,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "ERI+Fock quartets/s (C6H6 RHF/6-31G Fock build)"
 UNIT = "quartets/s"
-BATCH_LEVEL_SHIFT = 1.0  # Eh; SCF level shift of the batched water-cluster workload
+# SCF start of every bench workload: superposition of atomic densities (the
+# core guess leaves (H2O)32 and 2 of the 512 clusters unconverged), no level shift
+SCF_GUESS_NAME = "sad"
+BATCH_LEVEL_SHIFT = 0.0  # Eh
 MIXED_CURVE = (1.0, 0.1, 0.01, 1e-3, 1e-4)  # mixed thresholds of the batch's speed / accuracy curve
 BUILD_DRAM_BYTES_NCU = 25.0e6  # bytes per benzene FP64 build under ncu (launch list, 4 builds / 4)
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
@@ -169,7 +172,7 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
     from fock_gb300 import basis as B, molecules as M
     batch = M.water_cluster_batch(512, seed=0)
     mols = [B.build_atoms("6-31G", Zs, xyz) for Zs, xyz in batch]
-    kw = dict(guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, epsilon=1e-8, max_iters=100,
+    kw = dict(guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, epsilon=1e-8, max_iters=100,
               level_shift=BATCH_LEVEL_SHIFT, sign_convention=L.FOCK_SIGN_STANDARD, device=local)
     out = {"workload": "512 water clusters (H2O)_n, n~U{1..8} seed 0, RHF/6-31G, one batched context"}
     # warm-up: a 2-iteration batched SCF over one cluster of every size loads the
@@ -191,7 +194,7 @@ def batch_workload(torch, F, L, local, flush, steps=3, warmup=3, spot=6):
     out["scf_mixed"] = {"rc": rc, "wall_s": time.perf_counter() - t0, "fock_s": res[0].fock_seconds,
                         "fock_builds": res[0].fock_builds, "converged": sum(r.converged for r in res),
                         "iterations_max": max(r.iterations for r in res),
-                        "level_shift_eh": BATCH_LEVEL_SHIFT}
+                        "level_shift_eh": BATCH_LEVEL_SHIFT, "guess": SCF_GUESS_NAME}
     D = torch.zeros(b.total, dtype=torch.float64, device="cuda")
     for off, n, Dm in zip(b.offsets, b.nbf, dens):
         D[off:off + n * n] = torch.from_numpy(Dm.reshape(-1))
@@ -317,7 +320,7 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
         return out
     # mixed-precision SCF (final iterations FP64) and the nuclear gradient: analytic
     # derivative kernels for the s/p classes, finite-difference kernels for the d classes
-    with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
+    with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY,
                        energy_mode=1, epsilon=1e-8, max_iters=100, level_shift=BATCH_LEVEL_SHIFT,
                        device=local) as sctx:
         t0 = time.perf_counter()
@@ -328,9 +331,10 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
         g = sctx.energy_backward()
         grad_s = time.perf_counter() - t0
     out["scf_mixed"] = {"rc": rc, "wall_s": scf_s, "iterations": r.iterations, "energy": r.total_energy,
-                        "level_shift_eh": BATCH_LEVEL_SHIFT, "energy_per_water": r.total_energy / 32,
+                        "level_shift_eh": BATCH_LEVEL_SHIFT, "guess": SCF_GUESS_NAME,
+                        "energy_per_water": r.total_energy / 32,
                         "converged": bool(r.converged), "fock_builds": r.fock_builds, "fock_s": r.fock_seconds}
-    with F.FockContext(atoms, precision=L.FOCK_PREC_FP64, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY,
+    with F.FockContext(atoms, precision=L.FOCK_PREC_FP64, guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY,
                        energy_mode=1, epsilon=1e-8, max_iters=100, level_shift=BATCH_LEVEL_SHIFT,
                        device=local) as fctx:
         t0 = time.perf_counter()
@@ -353,7 +357,7 @@ def octane_gradient_workload(torch, F, L, local):
     from fock_gb300 import basis as B, molecules as M
     Zs, xyz = M.octane(seed=0)
     atoms = B.build_atoms("6-31G", Zs, xyz)
-    with F.FockContext(atoms, guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1,
+    with F.FockContext(atoms, guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1,
                        max_iters=100, epsilon=1e-10, device=local) as ctx:
         t0 = time.perf_counter()
         rc, r, eps, Dm, Cm = ctx.scf(0)
@@ -394,6 +398,30 @@ def orbital_grid_workload(torch, F, L, local, atoms, C, nocc, opts, steps=3, war
     return {"workload": "benzene HOMO on 200^3 voxels, box 20 bohr (volumetric viewer grid)",
             "ms_per_grid": ms, "voxels_per_s": nvox ** 3 / (ms * 1e-3), "functions_kept": nsel,
             "bytes_written": nvox ** 3 * 4}
+
+
+def profile_classes(torch, lib, ctx, D, flush, reps=3):
+    """Per-class launch times of one build, the classes launched one by one
+    (fock_profile_build), averaged over reps builds: {"(ab|cd)[f32]": {...}}."""
+    from fock_gb300 import _lib
+    cap = 512
+    arr = (_lib.LaunchProfile * cap)()
+    per_class = {}
+    for _ in range(reps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        np_ = lib.fock_profile_build(ctx.handle, C.c_void_p(D.data_ptr()), arr, cap)
+        for i in range(min(np_, cap)):
+            a = arr[i]
+            key = "(%d%d|%d%d)%s" % (a.la, a.lb, a.lc, a.ld, "" if a.prec == 0 else "f32")
+            d = per_class.setdefault(key, {"ms": 0.0, "flops": 0, "launches": 0, "prim_quartets": 0})
+            d["ms"] += a.ms / reps
+            d["flops"] += a.flops // reps
+            d["launches"] += 1
+            d["prim_quartets"] += a.prim_quartets // reps
+    for d in per_class.values():
+        d["launches"] //= reps
+    return per_class
 
 
 def run_reference_arm(args):
@@ -449,7 +477,7 @@ def main():
         print(json.dumps({args.only: fn()}), flush=True)
         return
     atoms = benzene_atoms()
-    opts = dict(guess=L.FOCK_GUESS_CORE, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, device=local,
+    opts = dict(guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, device=local,
                 sign_convention=L.FOCK_SIGN_STANDARD)
     extra = {}
     # one-time start-up (CUDA context, library tables, cuBLAS/cuSOLVER kernels) outside the SCF timings
@@ -464,7 +492,7 @@ def main():
         t0 = time.perf_counter()
         rmx = F.try_scf(atoms, 100, 1e-9, 0, precision=L.FOCK_PREC_MIXED, **opts)
         scfmx_s = time.perf_counter() - t0
-        extra["scf"] = {"fp64_wall_s": scf64_s, "fp64_iterations": r64.iterations, "fp64_energy": r64.total_energy,
+        extra["scf"] = {"guess": SCF_GUESS_NAME, "fp64_wall_s": scf64_s, "fp64_iterations": r64.iterations, "fp64_energy": r64.total_energy,
                         "fp64_fock_builds": r64.fock_builds, "fp64_fock_s": r64.fock_seconds,
                         "mixed_wall_s": scfmx_s, "mixed_iterations": rmx.iterations,
                         "mixed_energy": rmx.total_energy, "mixed_fock_s": rmx.fock_seconds,
@@ -513,25 +541,8 @@ def main():
 
     # ---- per-launch profile -> dominant kernel roofline ----
     from fock_gb300 import _lib
-    cap = 512
-
-    arr = (_lib.LaunchProfile * cap)()
     lib = _lib.lib()
-    per_class = {}
-    for _ in range(3):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        np_ = lib.fock_profile_build(ctx.handle, C.c_void_p(D.data_ptr()), arr, cap)
-        for i in range(min(np_, cap)):
-            a = arr[i]
-            key = "(%d%d|%d%d)%s" % (a.la, a.lb, a.lc, a.ld, "" if a.prec == 0 else "f32")
-            d = per_class.setdefault(key, {"ms": 0.0, "flops": 0, "launches": 0, "prim_quartets": 0})
-            d["ms"] += a.ms / 3.0
-            d["flops"] += a.flops // 3
-            d["launches"] += 1
-            d["prim_quartets"] += a.prim_quartets // 3
-    for d in per_class.values():
-        d["launches"] //= 3
+    per_class = profile_classes(torch, lib, ctx, D, flush)
     total_ms = sum(d["ms"] for d in per_class.values())
     dom_key = max(per_class, key=lambda k: per_class[k]["ms"])
     dom = per_class[dom_key]
@@ -575,6 +586,8 @@ def main():
     ms_mx = sum(tmx) / len(tmx)
     stm = ctx.stats()
     Gm = G.clone()
+    # per-class launch times of the mixed build (classes one by one): FP32 and FP64 shares
+    pc_mx = profile_classes(torch, lib, ctx, D, flush)
     ctx.set_precision(L.FOCK_PREC_FP64, th)
     ctx.build_jk_device(D.data_ptr(), G.data_ptr())
     stream.synchronize()
@@ -584,6 +597,7 @@ def main():
     mixed_frac = ((stm["flops_fp32"] / (fp32_peak_gflops.value * 1e9) + stm["flops_fp64"] / (peak * 1e12))
                   / (ms_mx * 1e-3)) if peak and fp32_peak_gflops.value else None
     mixed = {"value": nq / (ms_mx * 1e-3), "ms_per_step": ms_mx, "speedup_vs_fp64": ms / ms_mx,
+             "per_class_ms_serialised": {k: round(v["ms"], 4) for k, v in sorted(pc_mx.items())},
              "roofline_time_share_frac": mixed_frac,
              "mixed_threshold": th, "fp32_shell_quartets": stm["shell_quartets_fp32"],
              "fp64_shell_quartets": stm["shell_quartets_fp64"],

@@ -35,6 +35,7 @@ pub const FOCK_ERI_EXACT: c_int = 0;
 pub const FOCK_ERI_REFCOMPAT: c_int = 1;
 pub const FOCK_GUESS_GWH: c_int = 0;
 pub const FOCK_GUESS_CORE: c_int = 1;
+pub const FOCK_GUESS_SAD: c_int = 2;
 pub const FOCK_CONV_COMMUTATOR: c_int = 0;
 pub const FOCK_CONV_ENERGY: c_int = 1;
 pub const FOCK_NOALLOC_MAX_BASIS: c_int = 256;

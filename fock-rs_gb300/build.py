@@ -31,23 +31,35 @@ def _sources():
     return srcs
 
 
-def _deps_mtime():
-    m = 0.0
-    for root in (CSRC, GEN, os.path.join(os.path.dirname(HERE), "include")):
-        for f in os.listdir(root):
-            p = os.path.join(root, f)
-            if os.path.isfile(p) and f.endswith((".cu", ".cuh", ".h", ".py", ".inc")):
-                m = max(m, os.path.getmtime(p))
-    return m
+def _includes(path, seen):
+    """Quoted #include files of path, transitively (the files a translation unit depends on)."""
+    if path in seen or not os.path.isfile(path):
+        return
+    seen.add(path)
+    with open(path, errors="replace") as f:
+        for line in f:
+            t = line.strip()
+            if t.startswith("#include") and '"' in t:
+                name = t.split('"')[1]
+                _includes(os.path.normpath(os.path.join(os.path.dirname(path), name)), seen)
+
+
+def _deps_mtime(src):
+    seen = set()
+    _includes(src, seen)
+    return max(os.path.getmtime(p) for p in seen)
+
+
+def _flags():
+    return ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", CSRC, "--expt-relaxed-constexpr"] + \
+        os.environ.get("FOCK_GB300_NVCC_FLAGS", "").split()
 
 
 def _compile(src, verbose):
     obj = os.path.join(OBJ, os.path.basename(src) + ".o")
-    if os.path.exists(obj) and os.path.getmtime(obj) >= _deps_mtime():
+    if not verbose and os.path.exists(obj) and os.path.getmtime(obj) >= _deps_mtime(src):
         return obj
-    cmd = [nvcc()] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj,
-                             "-I", CSRC, "--expt-relaxed-constexpr"]
-    cmd += os.environ.get("FOCK_GB300_NVCC_FLAGS", "").split()
+    cmd = [nvcc()] + _flags() + ["-c", src, "-o", obj]
     if verbose:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -79,9 +91,33 @@ def build(verbose=False, jobs=None):
     import gen_eri  # noqa
     sys.path.pop(0)
     os.makedirs(GEN, exist_ok=True)
-    gen_eri.main(GEN, LMAX)
+    # generate into a scratch folder and copy only the files that changed, so
+    # that unchanged translation units keep their objects
+    tmp = GEN + ".tmp"
+    shutil.rmtree(tmp, ignore_errors=True)
+    gen_eri.main(tmp, LMAX)
+    fresh = set(os.listdir(tmp))
+    for f in os.listdir(GEN):
+        if f.startswith(("inst_", "cls_")) and f not in fresh:
+            os.remove(os.path.join(GEN, f))
+    for f in fresh:
+        new, old = os.path.join(tmp, f), os.path.join(GEN, f)
+        with open(new) as a:
+            text = a.read()
+        if not os.path.exists(old) or open(old).read() != text:
+            shutil.copyfile(new, old)
+    shutil.rmtree(tmp, ignore_errors=True)
     write_ref_lut()
     os.makedirs(OBJ, exist_ok=True)
+    # objects built with other flags are stale
+    stamp = os.path.join(OBJ, "flags.txt")
+    flags = " ".join(_flags())
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        for f in os.listdir(OBJ):
+            if f.endswith(".o"):
+                os.remove(os.path.join(OBJ, f))
+        with open(stamp, "w") as f:
+            f.write(flags)
     os.makedirs(LIBDIR, exist_ok=True)
     srcs = _sources()
     jobs = jobs or min(len(srcs), max(2, os.cpu_count() or 2))

@@ -22,6 +22,10 @@ constexpr int kBoysPts = 64 * kBoysPerUnit + 1;
 constexpr int kBoysTerms = 8;           // 7 Taylor coefficients + exp(-T_i)
 constexpr int kBoysTaylor = 7;
 constexpr int kBoysMaxM = 12;           // orders with a Taylor table
+// FP32 table: 16-byte rows of the first four coefficients (cubic Taylor
+// polynomial, truncation (1/64)^4/4! < 3e-9 relative), half the footprint of
+// the FP64 rows so that the order a class reads stays cache-resident
+constexpr int kBoysTerms32 = 4;
 constexpr double kBoysTmax = 64.0;
 constexpr float kBoysTmaxF = 64.0f;
 
@@ -63,13 +67,10 @@ struct __align__(16) PrimPair32 {
 // sum p among the distinct sums of the basis; entry (i, j) holds the
 // quantities of a primitive quartet that depend only on p_i and q_j:
 // {(p+q)^(-1/2), 1/(2(p+q)), q/(p+q) = rho/p, p/(p+q) = rho/q, rho = pq/(p+q)}
-// (FP64: precomputed so that the inner loop spends no FP64 instruction on
-// them; FP32 keeps the 16-byte form {rs, 1/(p+q), rho/p, rho/q}).
+// (precomputed so that the FP64 inner loop spends no FP64 instruction on
+// them; FP32 lanes compute them in registers, see PrimLoad<float>::exps).
 struct __align__(16) ExpPair64 {
   double rs, o2pq, rp, rq, rho, pad;
-};
-struct __align__(16) ExpPair32 {
-  float rs, inv, rp, rq;
 };
 
 // One launch of one class: rows are bra pairs; row r covers the kets
@@ -109,9 +110,8 @@ struct EriArgs {
   const PrimPair64* prim64;
   const PrimPair32* prim32;
   const double* boys64;   // [kBoysMaxM+1][kBoysPts][kBoysTerms]
-  const float* boys32;    // [kBoysMaxM+1][kBoysPts][kBoysTerms]
+  const float* boys32;    // [kBoysMaxM+1][kBoysPts][kBoysTerms32]
   const ExpPair64* xp64;  // [nxp][nxp]
-  const ExpPair32* xp32;
   int nxp;
   const double* D;        // density, nbf x nbf row-major (textbook sign convention)
   const float* D32;       // float copy for the FP32 digestion
@@ -250,7 +250,7 @@ __device__ __forceinline__ void boys_scaled(float T, float pref, const float* __
     int i = __float2int_rn(T * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
     const float d = fmaf((float)i, -1.0f / kBoysPerUnit, T);
-    const float4 c = __ldg(reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysPts + i) * kBoysTerms));
+    const float4 c = __ldg(reinterpret_cast<const float4*>(tab + ((size_t)L * kBoysPts + i) * kBoysTerms32));
     float f = fmaf(c.w, d, c.z);
     f = fmaf(f, d, c.y);
     f = fmaf(f, d, c.x);

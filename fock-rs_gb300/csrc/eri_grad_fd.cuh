@@ -58,7 +58,7 @@ __device__ __noinline__ double quartet_energy(const EriArgs& a, const PairInfo& 
       kp.load(a, Pk.prim_off + ik);
       if (which == 2) displace_prim(a, Pk.prim_off + ik, Pk.AB, 0, axis, h, kp);
       double rs, o2pq, rp, rq, rho;
-      bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
+      bp.exps(a, kp, rs, o2pq, rp, rq, rho);
       const double PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const double r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
       double F[L + 1];

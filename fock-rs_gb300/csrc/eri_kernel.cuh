@@ -53,10 +53,11 @@ struct PrimLoad<double> {
     const double2* v = a.prim64[idx].v;
     set(__ldg(v), __ldg(v + 1), __ldg(v + 2), __ldg(v + 3), __ldg(v + 4));
   }
-  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho for this bra exponent sum and eid_k
-  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, double& rs, double& o2pq, double& rp,
-                                       double& rq, double& rho) const {
-    const double2* x = reinterpret_cast<const double2*>(a.xp64 + (size_t)eid * a.nxp + eid_k);
+  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho of this bra and the ket k,
+  // from the exponent-sum table (no FP64-pipe work)
+  __device__ __forceinline__ void exps(const EriArgs& a, const PrimLoad<double>& k, double& rs, double& o2pq,
+                                       double& rp, double& rq, double& rho) const {
+    const double2* x = reinterpret_cast<const double2*>(a.xp64 + (size_t)eid * a.nxp + k.eid);
     const double2 x0 = __ldg(x), x1 = __ldg(x + 1);
     rs = x0.x; o2pq = x0.y; rp = x1.x; rq = x1.y;
     rho = __ldg(reinterpret_cast<const double*>(x + 2));
@@ -66,20 +67,29 @@ struct PrimLoad<double> {
 template <>
 struct PrimLoad<float> {
   float p, o2p, K, P[3], PA[3];
-  int eid;
   __device__ __forceinline__ void set(float4 v0, float4 v1, float4 v2) {
     p = v0.x; o2p = v0.y; K = v0.z; P[0] = v0.w; P[1] = v1.x; P[2] = v1.y;
     PA[0] = v1.z; PA[1] = v1.w; PA[2] = v2.x;
-    eid = __float_as_int(v2.y);
   }
   __device__ __forceinline__ void load(const EriArgs& a, int idx) {
     const float4* v = a.prim32[idx].v;
     set(__ldg(v), __ldg(v + 1), __ldg(v + 2));
   }
-  __device__ __forceinline__ void exps(const EriArgs& a, int eid_k, float& rs, float& o2pq, float& rp,
+  // the same quantities computed in registers: FP32 lanes are bound by their
+  // gathers, not by the FP32 pipe, so a few FP32/MUFU instructions replace the
+  // table gather.  1/s is correctly rounded (__frcp_rn); s^(-1/2) is the
+  // hardware estimate refined by one Newton step y (1 + e/2), e = 1 - s y^2,
+  // so both carry about the rounding error of the table entries.
+  __device__ __forceinline__ void exps(const EriArgs&, const PrimLoad<float>& k, float& rs, float& o2pq, float& rp,
                                        float& rq, float& rho) const {
-    const float4 x = __ldg(reinterpret_cast<const float4*>(a.xp32 + (size_t)eid * a.nxp + eid_k));
-    rs = x.x; o2pq = 0.5f * x.y; rp = x.z; rq = x.w;
+    const float sum = p + k.p;
+    const float inv = __frcp_rn(sum);
+    const float y = rsqrtf(sum);
+    const float e = fmaf(-sum * y, y, 1.0f);
+    rs = fmaf(0.5f * y, e, y);
+    o2pq = 0.5f * inv;
+    rp = k.p * inv;
+    rq = p * inv;
     rho = p * rp;
   }
 };
@@ -162,18 +172,31 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   if (MODE == MODE_SCHWARZ) {
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
+  } else if (MODE == MODE_JK) {
+    // idle lanes: past the launch's end, or quartets on the other side of a
+    // density-weighted split.  In FP32 warps with work they stay to the end
+    // (the J_ab reduction below is a warp collective) with no primitive work.
+    active = t < cl.nlanes;
+    if (active) {
+      int row, kloc;
+      decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc);
+      if (cl.row_split && kloc < __ldg(cl.row_split + row)) {
+        // density-weighted precision split: this launch keeps its side of the bound
+        const PairInfo& Pb = a.pairs[bra];
+        const PairInfo& Pk = a.pairs[ket];
+        const float w = quartet_dmax<C>(a, (size_t)Pb.mol_off, Pb.mol_n, Pb.fa, Pb.fb, Pk.fa, Pk.fb);
+        const bool heavy = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), w) >= cl.wthr;
+        active = heavy == (sizeof(R) == sizeof(double));
+      }
+    } else {
+      bra = ket = __ldg(cl.bra_list);
+    }
+    // FP64 lanes take part in no warp collective and leave at once; FP32
+    // warps leave together when none of their lanes has work
+    if (sizeof(R) == sizeof(double) ? !active : __ballot_sync(0xffffffffu, active) == 0u) return;
   } else {
     if (t >= cl.nlanes) return;  // only the launch's last warp has idle lanes
-    int row, kloc;
-    decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc);
-    if (MODE == MODE_JK && cl.row_split && kloc < __ldg(cl.row_split + row)) {
-      // density-weighted precision split: this launch keeps its side of the bound
-      const PairInfo& Pb = a.pairs[bra];
-      const PairInfo& Pk = a.pairs[ket];
-      const float w = quartet_dmax<C>(a, (size_t)Pb.mol_off, Pb.mol_n, Pb.fa, Pb.fb, Pk.fa, Pk.fb);
-      const bool heavy = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), w) >= cl.wthr;
-      if (heavy != (sizeof(R) == sizeof(double))) return;
-    }
+    decode_lane(cl, t, bra, ket, slice, nslice);
     active = true;
   }
   const PairInfo& Pb = a.pairs[bra];
@@ -187,7 +210,7 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
     // work actually computed (the split is decided per build): one atomic per warp
     const unsigned m = __activemask();
     const unsigned pq = __reduce_add_sync(m, (unsigned)((ib1 - ib0) * nkp));
-    const unsigned q = __reduce_add_sync(m, slice == 0 ? 1u : 0u);
+    const unsigned q = __reduce_add_sync(m, (active && slice == 0) ? 1u : 0u);
     if ((threadIdx.x & 31) == __ffs(m) - 1) {
       atomicAdd(cl.counters, (unsigned long long)q);
       atomicAdd(cl.counters + 1, (unsigned long long)pq);
@@ -203,15 +226,24 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   // (scattered: every lane of a warp has its own ket) are read once per slice,
   // while the bra records of the inner loop are the same for all lanes of a
   // row and load as broadcasts
+  // FP32 lanes load the next ket record while the current one's bra loop runs
+  constexpr bool kPrefetch = sizeof(R) == sizeof(float);
+  PrimLoad<R> knext;
+  if (kPrefetch && nkp > 0) knext.load(a, kp0);
   for (int ik = 0; ik < nkp; ++ik) {
     PrimLoad<R> kp;
-    kp.load(a, kp0 + ik);
+    if (kPrefetch) {
+      kp = knext;
+      if (ik + 1 < nkp) knext.load(a, kp0 + ik + 1);
+    } else {
+      kp.load(a, kp0 + ik);
+    }
 #pragma unroll kKetUnroll
     for (int ib = ib0; ib < ib1; ++ib) {
       PrimLoad<R> bp;
       bp.load(a, bp0 + ib);
       R rs, o2pq, rp, rq, rho;  // (p+q)^(-1/2), 1/(2(p+q)), rho/p, rho/q, rho from the exponent-sum table
-      bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
+      bp.exps(a, kp, rs, o2pq, rp, rq, rho);
       const R PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const R r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
       const R T = rho * r2;
@@ -339,9 +371,53 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   // scaling runs in the lane's own precision (FP32 lanes issue no FP64-pipe op)
   const R sdeg = (Pb.sa == Pb.sb ? R(0.5) : R(1)) * (Pk.sa == Pk.sb ? R(0.5) : R(1)) * (bra == ket ? R(0.5) : R(1));
   const R sj = R(2) * sdeg, sk = R(-0.5) * sdeg;
-  if (!active) return;
+  if (sizeof(R) == sizeof(float)) {
+    // FP32 lanes that share the bra pair (a warp usually covers the kets of
+    // one row) add their sj J_ab blocks first: a segmented tree reduction over
+    // the runs of equal bra in the warp, after which the run's first lane
+    // alone adds to M_ab (one atomic per element instead of one per lane on
+    // the same address).  The sums are compensated (Knuth's TwoSum: value +
+    // rounding error, both floats) and both parts go to the FP64 accumulator,
+    // so the result does not depend on how lanes fall into warps beyond FP64
+    // rounding, and no FP64-pipe instruction is spent.
+    const unsigned lane = threadIdx.x & 31u;
+    const int key = active ? bra : -1 - (int)lane;
+    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
+    const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != key);
+    R jlo[NA * NB];
 #pragma unroll
-  for (int i = 0; i < NA * NB; ++i) atomicAdd(a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB), to_f64(sj * jab[i]));
+    for (int i = 0; i < NA * NB; ++i) { jab[i] *= sj; jlo[i] = R(0); }
+    if (heads != 0xffffffffu) {  // some run is longer than one lane
+      const unsigned above = heads & (0xfffffffeu << lane);  // run heads after this lane
+      const int seg_end = above ? __ffs(above) - 2 : 31;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const bool take = (int)lane + off <= seg_end;
+#pragma unroll
+        for (int i = 0; i < NA * NB; ++i) {
+          const R hi = __shfl_down_sync(0xffffffffu, jab[i], off);
+          const R lo = __shfl_down_sync(0xffffffffu, jlo[i], off);
+          if (take) {
+            const R sum = jab[i] + hi, bb = sum - jab[i];
+            jlo[i] += lo + ((jab[i] - (sum - bb)) + (hi - bb));
+            jab[i] = sum;
+          }
+        }
+      }
+    }
+    if (!active) return;
+    if ((heads >> lane) & 1u) {
+#pragma unroll
+      for (int i = 0; i < NA * NB; ++i) {
+        double* m = a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB);
+        atomicAdd(m, to_f64(jab[i]));
+        atomicAdd(m, to_f64(jlo[i]));
+      }
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < NA * NB; ++i) atomicAdd(a.M + mo + (size_t)(fa + i / NB) * ld + (fb + i % NB), to_f64(sj * jab[i]));
+  }
 #pragma unroll
   for (int ic = 0; ic < NC; ++ic)
 #pragma unroll
@@ -432,7 +508,7 @@ __global__ void __launch_bounds__(kEriThreads) eri_grad_kernel(const ClassLaunch
       kp.load(a, Pk.prim_off + ik);
       const double wc = 2.0 * __ldg(&a.prim64[Pk.prim_off + ik].v[5].x);
       double rs, o2pq, rp, rq, rho;
-      bp.exps(a, kp.eid, rs, o2pq, rp, rq, rho);
+      bp.exps(a, kp, rs, o2pq, rp, rq, rho);
       const double PQ[3] = {bp.P[0] - kp.P[0], bp.P[1] - kp.P[1], bp.P[2] - kp.P[2]};
       const double r2 = PQ[0] * PQ[0] + PQ[1] * PQ[1] + PQ[2] * PQ[2];
       const double T = rho * r2;

@@ -24,6 +24,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/fock_gb300.h"
@@ -63,7 +64,7 @@ inline int ncart(int l) { return (l + 1) * (l + 2) / 2; }
 
 // ---------------------------------------------------------------------------
 // Boys tables (host generation, once per process).
-// F_n(T_i), T_i = i/16, from the power series
+// F_n(T_i), T_i = i/32, from the power series
 //   F_n(T) = e^{-T} sum_k (2T)^k / ((2n+1)(2n+3)...(2n+2k+1))
 // (positive terms, no cancellation) for the top order in long double, then
 // the stable downward recursion F_{n-1} = (2T F_n + e^{-T}) / (2n-1).
@@ -97,7 +98,7 @@ void build_tables() {
     }
   }
   g_boys64.assign((size_t)(kBoysMaxM + 1) * kBoysPts * kBoysTerms, 0.0);
-  g_boys32.assign(g_boys64.size(), 0.0f);
+  g_boys32.assign((size_t)(kBoysMaxM + 1) * kBoysPts * kBoysTerms32, 0.0f);
   for (int M = 0; M <= kBoysMaxM; ++M)
     for (int i = 0; i < kBoysPts; ++i) {
       long double fact = 1.0L;
@@ -107,11 +108,10 @@ void build_tables() {
         long double c = F[(size_t)i * (kTabOrders + 1) + M + k] / fact;
         if (k & 1) c = -c;
         g_boys64[row + k] = (double)c;
-        g_boys32[row + k] = (float)c;
+        if (k < kBoysTerms32) g_boys32[((size_t)M * kBoysPts + i) * kBoysTerms32 + k] = (float)c;
       }
       const long double ex = expl(-(long double)i / (long double)kBoysPerUnit);
       g_boys64[row + kBoysTaylor] = (double)ex;
-      g_boys32[row + kBoysTaylor] = (float)ex;
     }
   // reference LUT: F_10(0.15 k), k < 200, the values stored in boys/src/lut.rs
   g_ref_lut.assign(kRefBoysLut, kRefBoysLut + 200);
@@ -212,7 +212,6 @@ struct fock_ctx {
   PrimPair32* d_prim32 = nullptr;
   double *d_boys64 = nullptr, *d_ref_lut = nullptr;
   ExpPair64* d_xp64 = nullptr;
-  ExpPair32* d_xp32 = nullptr;
   int nxp = 0;
   float* d_boys32 = nullptr;
   float* d_schwarz = nullptr;
@@ -267,7 +266,6 @@ EriArgs eri_args(fock_ctx* c) {
   a.boys64 = c->d_boys64;
   a.boys32 = c->d_boys32;
   a.xp64 = c->d_xp64;
-  a.xp32 = c->d_xp32;
   a.nxp = c->nxp;
   a.D = c->d_D;
   a.D32 = c->d_D32;
@@ -766,7 +764,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
-  dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64); dfree(c->d_xp32);
+  dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64);
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
   dfree(c->d_plan_int); dfree(c->d_plan_ll);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
@@ -939,7 +937,6 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
     p32[k].v[2].y = idf;
   }
   std::vector<ExpPair64> xp64((size_t)c->nxp * c->nxp);
-  std::vector<ExpPair32> xp32(xp64.size());
   for (int i = 0; i < c->nxp; ++i)
     for (int j = 0; j < c->nxp; ++j) {
       const long double p = psum[i], q = psum[j], s = p + q;
@@ -950,7 +947,6 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       e.rq = (double)(p / s);
       e.rho = (double)(p * q / s);
       e.pad = 0.0;
-      xp32[(size_t)i * c->nxp + j] = ExpPair32{(float)e.rs, (float)(1.0L / s), (float)e.rp, (float)e.rq};
     }
   const int npairs = (int)c->hpairs.size();
   const size_t nn = (size_t)c->total_elems;  // all molecule blocks
@@ -960,7 +956,6 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       (rc = map_cuda(dalloc(&c->d_boys64, g_boys64.size()))) ||
       (rc = map_cuda(dalloc(&c->d_boys32, g_boys32.size()))) ||
       (rc = map_cuda(dalloc(&c->d_xp64, xp64.size()))) ||
-      (rc = map_cuda(dalloc(&c->d_xp32, xp32.size()))) ||
       (rc = map_cuda(dalloc(&c->d_ref_lut, g_ref_lut.size()))) ||
       (rc = map_cuda(dalloc(&c->d_schwarz, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_D, nn))) || (rc = map_cuda(dalloc(&c->d_M, nn))) ||
@@ -972,7 +967,6 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       (rc = map_cuda(cudaMemcpy(c->d_boys64, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_boys32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_xp64, xp64.data(), xp64.size() * sizeof(ExpPair64), cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_xp32, xp32.data(), xp32.size() * sizeof(ExpPair32), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_ref_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice))))
     return fail(rc);
 
@@ -1646,6 +1640,199 @@ int fock_measure_fma_peak(int device, int fp64, double* gflops) {
   return FOCK_OK;
 }
 
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Superposition-of-atomic-densities (SAD) guess.  Each distinct atom (element
+// and shells) gets the density of a spherically averaged RHF of the free atom:
+// Roothaan iterations in which the orbitals fill in energy order and a group of
+// degenerate orbitals that the remaining electrons cannot fill shares them
+// equally (O: 1s^2 2s^2 2p^{4/3 x 3}; H: 1s^1), which keeps the atom's density
+// spherical.  The Fock builds run on the device through a one-atom context;
+// the small matrix algebra runs on the host.  The molecular guess is the
+// block-diagonal sum of the atoms' densities, so every atom starts neutral.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Eigenvalues (ascending) and eigenvectors (column k of V, row-major n x n) of
+// a small symmetric matrix by the cyclic Jacobi method (Golub and Van Loan,
+// Matrix Computations, section 8.5).
+void jacobi_eigh(int n, std::vector<double> A, std::vector<double>& w, std::vector<double>& V) {
+  V.assign((size_t)n * n, 0.0);
+  for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) (i == j ? tot : off) += A[(size_t)i * n + j] * A[(size_t)i * n + j];
+    if (off <= 1e-30 * (tot + off)) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = A[(size_t)p * n + q];
+        if (apq == 0.0) continue;
+        const double theta = (A[(size_t)q * n + q] - A[(size_t)p * n + p]) / (2.0 * apq);
+        const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+        for (int k = 0; k < n; ++k) {  // A <- A J (columns p, q)
+          const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+          A[(size_t)k * n + p] = cs * akp - sn * akq;
+          A[(size_t)k * n + q] = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // A <- J^T A (rows p, q)
+          const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+          A[(size_t)p * n + k] = cs * apk - sn * aqk;
+          A[(size_t)q * n + k] = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < n; ++k) {  // V <- V J
+          const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+          V[(size_t)k * n + p] = cs * vkp - sn * vkq;
+          V[(size_t)k * n + q] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  std::vector<int> ord(n);
+  for (int i = 0; i < n; ++i) ord[i] = i;
+  std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return A[(size_t)x * n + x] < A[(size_t)y * n + y]; });
+  std::vector<double> V2((size_t)n * n);
+  w.resize(n);
+  for (int k = 0; k < n; ++k) {
+    w[k] = A[(size_t)ord[k] * n + ord[k]];
+    for (int i = 0; i < n; ++i) V2[(size_t)i * n + k] = V[(size_t)i * n + ord[k]];
+  }
+  V.swap(V2);
+}
+
+// Spherically averaged RHF density of one free atom (row-major n x n, textbook
+// sign convention) for the given shells, all on atom 0 at the origin.
+int atom_density(int Z, const std::vector<fock_shell>& shells, int device, std::vector<double>& Dout) {
+  fock_options o;
+  fock_options_default(&o);
+  o.sign_convention = FOCK_SIGN_STANDARD;
+  o.device = device;
+  const fock_atom at{0.0, 0.0, 0.0, Z};
+  const int begin[2] = {0, (int)shells.size()};
+  fock_ctx* ac = nullptr;
+  int rc = create_ctx(&at, 1, shells.data(), (int)shells.size(), &o, begin, 1, &ac);
+  if (rc != FOCK_OK) return rc;
+  const int n = ac->nbf;
+  const size_t nn = (size_t)n * n;
+  std::vector<double> S(nn), T(nn), V(nn), H(nn), G(nn), F(nn), D(nn, 0.0), X(nn), w, U, C(nn);
+  rc = fock_one_electron(ac, S.data(), T.data(), V.data());
+  if (rc != FOCK_OK) { fock_ctx_destroy(ac); return rc; }
+  for (size_t i = 0; i < nn; ++i) H[i] = T[i] + V[i];
+  // Loewdin X = U diag(s^-1/2) U^T
+  jacobi_eigh(n, S, w, U);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      double x = 0.0;
+      for (int k = 0; k < n; ++k) x += U[(size_t)i * n + k] * U[(size_t)j * n + k] / std::sqrt(w[k]);
+      X[(size_t)i * n + j] = x;
+    }
+  F = H;
+  double e_prev = 0.0;
+  for (int it = 0; it < 100; ++it) {
+    // F' = X F X, C = X C'
+    std::vector<double> XF(nn, 0.0), Fp(nn, 0.0);
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) XF[(size_t)i * n + j] += X[(size_t)i * n + k] * F[(size_t)k * n + j];
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) Fp[(size_t)i * n + j] += XF[(size_t)i * n + k] * X[(size_t)k * n + j];
+    std::vector<double> eps, Cp;
+    jacobi_eigh(n, Fp, eps, Cp);
+    std::fill(C.begin(), C.end(), 0.0);
+    for (int i = 0; i < n; ++i)
+      for (int k = 0; k < n; ++k)
+        for (int j = 0; j < n; ++j) C[(size_t)i * n + j] += X[(size_t)i * n + k] * Cp[(size_t)k * n + j];
+    // occupations: energy order, degenerate groups share what is left
+    std::vector<double> occ(n, 0.0);
+    double left = Z;
+    for (int k = 0; k < n && left > 0.0;) {
+      int g = 1;
+      while (k + g < n && std::fabs(eps[k + g] - eps[k]) < 1e-5 * std::max(1.0, std::fabs(eps[k]))) ++g;
+      const double take = std::min(2.0 * g, left);
+      for (int q = 0; q < g; ++q) occ[k + q] = take / g;
+      left -= take;
+      k += g;
+    }
+    double dmax = 0.0;
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) {
+        double d = 0.0;
+        for (int k = 0; k < n; ++k) d += occ[k] * C[(size_t)i * n + k] * C[(size_t)j * n + k];
+        dmax = std::max(dmax, std::fabs(d - D[(size_t)i * n + j]));
+        D[(size_t)i * n + j] = d;
+      }
+    rc = fock_build_jk(ac, D.data(), G.data());
+    if (rc != FOCK_OK) break;
+    double e = 0.0;
+    for (size_t i = 0; i < nn; ++i) {
+      F[i] = H[i] + G[i];
+      e += 0.5 * D[i] * (H[i] + F[i]);
+    }
+    if (it > 0 && dmax < 1e-7 && std::fabs(e - e_prev) < 1e-9) break;
+    e_prev = e;
+  }
+  fock_ctx_destroy(ac);
+  if (rc != FOCK_OK) return rc;
+  Dout.swap(D);
+  return FOCK_OK;
+}
+
+// The SAD density of every molecule of the context: its n x n blocks at
+// mol_off (textbook sign convention, symmetric).
+int sad_density(fock_ctx* c, std::vector<double>& Dall) {
+  Dall.assign((size_t)c->total_elems, 0.0);
+  // shells of every atom, in context order; atoms with equal element and
+  // shells share one atomic calculation
+  std::vector<std::vector<int>> atom_shells(c->natom);
+  for (int s = 0; s < (int)c->shells.size(); ++s) atom_shells[c->shells[s].atom].push_back(s);
+  std::map<std::vector<double>, std::vector<double>> cache;
+  for (int a = 0; a < c->natom; ++a) {
+    const std::vector<int>& sl = atom_shells[a];
+    if (sl.empty()) continue;
+    std::vector<double> key{(double)c->atoms[a].Z};
+    std::vector<fock_shell> fs;
+    std::vector<std::vector<double>> raw(sl.size());
+    for (size_t q = 0; q < sl.size(); ++q) {
+      const HostShell& h = c->shells[sl[q]];
+      key.push_back(1000.0 + h.l);
+      for (int k = 0; k < h.nprim; ++k) {
+        raw[q].push_back(h.coefs[k] / prim_norm(h.l, 0, 0, h.exps[k]));
+        key.push_back(h.exps[k]);
+        key.push_back(raw[q].back());
+      }
+    }
+    for (size_t q = 0; q < sl.size(); ++q) {
+      const HostShell& h = c->shells[sl[q]];
+      fs.push_back(fock_shell{h.l, h.nprim, 0, h.exps.data(), raw[q].data()});
+    }
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+      std::vector<double> Da;
+      int rc = atom_density(c->atoms[a].Z, fs, c->device, Da);
+      if (rc != FOCK_OK) return rc;
+      it = cache.emplace(key, std::move(Da)).first;
+    }
+    const std::vector<double>& Da = it->second;
+    // local function index -> index within the molecule
+    std::vector<int> fmap;
+    for (int s : sl)
+      for (int k = 0; k < ncart(c->shells[s].l); ++k) fmap.push_back(c->shells[s].f0 + k);
+    const int na = (int)fmap.size();
+    const int m = c->shells[sl[0]].mol;
+    const int nm = c->mol_nbf[m];
+    double* blk = Dall.data() + c->mol_off[m];
+    for (int i = 0; i < na; ++i)
+      for (int j = 0; j < na; ++j) blk[(size_t)fmap[i] * nm + fmap[j]] = Da[(size_t)i * na + j];
+  }
+  return FOCK_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 // ---------------------------------------------------------------------------
 // RHF (scf/src/lib.rs:73-258) on the device.  Column-major n x n buffers.
 // ---------------------------------------------------------------------------
@@ -1788,9 +1975,17 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
       cku(cudaMemsetAsync(Dout, 0, nn * 8, s));
     }
   };
-  cku(k_guess(S, H, F, n, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, s));
-  c->launches++;
-  density_from(F, Dm);
+  if (c->opt.guess == FOCK_GUESS_SAD) {  // the first Fock matrix comes from the atoms' densities
+    std::vector<double> hD;
+    int r = sad_density(c, hD);
+    if (r != FOCK_OK) { cleanup(); return r; }
+    cku(cudaMemcpyAsync(Dm, hD.data(), nn * 8, cudaMemcpyHostToDevice, s));
+    cku(cudaStreamSynchronize(s));
+  } else {
+    cku(k_guess(S, H, F, n, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, s));
+    c->launches++;
+    density_from(F, Dm);
+  }
   if (fail != FOCK_OK) { cleanup(); return fail; }
   // FOCK_GB300_TRACE=1: per-phase host wall times of this SCF on stderr
   // (set-up; per iteration: Fock build, DIIS algebra, eigensolve + density, energy read-back)
@@ -2046,6 +2241,9 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     double err;
     std::memcpy(&err, &bits, 8);
     const double e_cur = hs[0], e_ref = hs[1];
+    if (trace)
+      std::fprintf(stderr, "fock_scf iter %d: E %.10f, max|FDS - SDF| %.3e, shift %.3f%s\n", iter, e_cur + vnn, err,
+                   shift_now, fp64_phase || !mixed ? "" : " (mixed)");
     err_prev = err;
     bool done;
     if (c->opt.conv_mode == FOCK_CONV_COMMUTATOR) done = err < c->opt.epsilon;
@@ -2374,9 +2572,17 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
       }
     }
   };
-  cku(kb_guess(S, H, c->d_mol_off, c->d_mol_n, nmol, T, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, F, s));
-  c->launches++;
-  density_from(F, Dm);
+  if (c->opt.guess == FOCK_GUESS_SAD) {
+    std::vector<double> hD;
+    int r = sad_density(c, hD);
+    if (r != FOCK_OK) { cleanup(); return r; }
+    cku(cudaMemcpyAsync(Dm, hD.data(), (size_t)T * 8, cudaMemcpyHostToDevice, s));
+    cku(cudaStreamSynchronize(s));
+  } else {
+    cku(kb_guess(S, H, c->d_mol_off, c->d_mol_n, nmol, T, c->opt.guess == FOCK_GUESS_GWH ? 1 : 0, F, s));
+    c->launches++;
+    density_from(F, Dm);
+  }
 
   // Per-molecule plan state: 1 = mixed precision, 2 = FP64, 0 = out of the
   // plan (converged, result frozen).  A mixed molecule becomes "ready" once its

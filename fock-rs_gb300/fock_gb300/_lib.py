@@ -13,7 +13,7 @@ FOCK_OK = 0
 FOCK_SIGN_REFERENCE, FOCK_SIGN_STANDARD = 0, 1
 FOCK_PREC_FP64, FOCK_PREC_MIXED = 0, 1
 FOCK_ERI_EXACT, FOCK_ERI_REFCOMPAT = 0, 1
-FOCK_GUESS_GWH, FOCK_GUESS_CORE = 0, 1
+FOCK_GUESS_GWH, FOCK_GUESS_CORE, FOCK_GUESS_SAD = 0, 1, 2
 FOCK_CONV_COMMUTATOR, FOCK_CONV_ENERGY = 0, 1
 FOCK_BOYS_FP64, FOCK_BOYS_FP32, FOCK_BOYS_REFERENCE, FOCK_BOYS_MD = 0, 1, 2, 3
 FOCK_ERR_INVALID_ARG, FOCK_ERR_UNSUPPORTED_L, FOCK_ERR_OOM = -1, -2, -3

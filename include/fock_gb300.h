@@ -54,6 +54,10 @@ extern "C" {
 
 #define FOCK_GUESS_GWH 0  /* 0.875 S_ij (H_ii + H_jj), scf/src/lib.rs:150-162 */
 #define FOCK_GUESS_CORE 1 /* F = H */
+#define FOCK_GUESS_SAD 2  /* superposition of atomic densities: each atom's density from a
+                             spherically averaged RHF of the free atom (no reference
+                             counterpart; for large clusters, where the core and GWH
+                             guesses slosh charge between molecules) */
 
 #define FOCK_CONV_COMMUTATOR 0 /* max|FDS - SDF| < epsilon, scf/src/lib.rs:191-192,224 */
 #define FOCK_CONV_ENERGY 1     /* |E_k - E_{k-1}| < epsilon and max|FDS-SDF| < sqrt(epsilon) */
