@@ -350,6 +350,50 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
     return out
 
 
+def shard_balance_workload(torch, F, L, local, flush, steps=3, warmup=2, ks=(2, 4, 8)):
+    """Row shards of the (H2O)32 / 6-31G* FP64 build (the multi-GPU split: rows
+    r % k == rank, one all-reduce of G per build), measured on this one GPU:
+    every shard's build time and quartet counts, run one after another.  The
+    slowest shard bounds a k-GPU build; the all-reduce of the 608 x 608 G
+    (2.96 MB) is not included."""
+    from fock_gb300 import basis as B, molecules as M
+    Zs, xyz = M.water_cluster(32, seed=0)
+    atoms = B.build_atoms("6-31G*", Zs, xyz)
+    stream = torch.cuda.Stream()
+    out = {"workload": "(H2O)32 seed 0, RHF/6-31G*, FP64 build, row shards r % k on one GPU"}
+    D = G = None
+    full_ms = None
+    for k in (1,) + tuple(ks):
+        shards = []
+        for r in range(k):
+            with F.FockContext(atoms, sign_convention=L.FOCK_SIGN_STANDARD, device=local, shard_index=r,
+                               shard_count=k) as ctx:
+                if D is None:
+                    n = ctx.n
+                    rng = np.random.default_rng(0)
+                    Cm = rng.normal(size=(n, 160)) / np.sqrt(n)
+                    D = torch.tensor(2.0 * Cm @ Cm.T, device="cuda")
+                    G = torch.empty_like(D)
+                ctx.set_stream(stream.cuda_stream)
+                t = _event_times(torch, stream, lambda: ctx.build_jk_device(D.data_ptr(), G.data_ptr()), steps,
+                                 warmup, flush)
+                st = ctx.stats()
+                shards.append({"ms": sum(t) / len(t), "shell_quartets": st["shell_quartets_fp64"],
+                               "prim_quartets": st["prim_quartets_fp64"], "flops": st["flops_fp64"]})
+        ms = [x["ms"] for x in shards]
+        fl = [x["flops"] for x in shards]
+        if k == 1:
+            full_ms = ms[0]
+            out["full_build_ms"] = full_ms
+            continue
+        out["k%d" % k] = {"shard_ms": [round(x, 3) for x in ms],
+                          "max_over_mean_ms": max(ms) / (sum(ms) / k),
+                          "max_over_mean_flops": max(fl) / (sum(fl) / k),
+                          "shell_quartets": [x["shell_quartets"] for x in shards],
+                          "projected_speedup": full_ms / max(ms)}
+    return out
+
+
 def octane_gradient_workload(torch, F, L, local):
     """n-octane C8H18 (seed 0, sigma 0.05 A), RHF/6-31G: FP64 SCF, then the
     nuclear gradient through fock_energy_backward (derivative ERIs contracted
@@ -424,6 +468,10 @@ def profile_classes(torch, lib, ctx, D, flush, reps=3):
     return per_class
 
 
+def parallelism(world):
+    return "row shards (r %% %d) + NCCL all-reduce of G" % world if world > 1 else "single"
+
+
 def run_reference_arm(args):
     rank, world, _ = env_rank()
     if rank != 0:
@@ -433,8 +481,9 @@ def run_reference_arm(args):
     cb["unit"] = UNIT
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * WORKLOAD["unique_quartets"] / value,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single"), "cpu_baseline": cb,
+            "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "config": dict(WORKLOAD, parallelism=parallelism(world)),
+            "cpu_baseline": cb,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -448,7 +497,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scf", action="store_true")
     ap.add_argument("--no-extra", action="store_true", help="skip the batch, (H2O)32 and gradient workloads")
-    ap.add_argument("--only", choices=["benzene", "benzene_mixed", "batch", "water32", "water32_builds", "octane"],
+    ap.add_argument("--only", choices=["benzene", "benzene_mixed", "batch", "water32", "water32_builds", "octane",
+                                       "shards"],
                     help="run one side workload alone (profiling) and print its JSON")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
@@ -473,7 +523,8 @@ def main():
               "water32_builds": lambda: water32_workload(torch, F, L, local, flush, args.steps, args.warmup, True),
               "batch": lambda: batch_workload(torch, F, L, local, flush, args.steps, args.warmup),
               "water32": lambda: water32_workload(torch, F, L, local, flush, args.steps, args.warmup),
-              "octane": lambda: octane_gradient_workload(torch, F, L, local)}[args.only]
+              "octane": lambda: octane_gradient_workload(torch, F, L, local),
+              "shards": lambda: shard_balance_workload(torch, F, L, local, flush)}[args.only]
         print(json.dumps({args.only: fn()}), flush=True)
         return
     atoms = benzene_atoms()
@@ -497,7 +548,10 @@ def main():
                         "mixed_wall_s": scfmx_s, "mixed_iterations": rmx.iterations,
                         "mixed_energy": rmx.total_energy, "mixed_fock_s": rmx.fock_seconds,
                         "abs_energy_error_mixed_vs_fp64_eh": abs(rmx.total_energy - r64.total_energy)}
-    ctx = F.FockContext(atoms, **opts)
+    # under torchrun every rank builds its row shard of the quartet plan (rows
+    # r % world == rank) and one all-reduce of G per build completes it
+    shard = dict(shard_index=rank, shard_count=world) if world > 1 else {}
+    ctx = F.FockContext(atoms, **opts, **shard)
     stream = torch.cuda.Stream()
     ctx.set_stream(stream.cuda_stream)
     n = ctx.n
@@ -506,15 +560,20 @@ def main():
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     nq = WORKLOAD["unique_quartets"]
 
+    def one_build():
+        ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+        if dist:
+            dist.all_reduce(G)  # partial G of the row shards -> G (on the current stream)
+
     def timed_builds(k, w):
         with torch.cuda.stream(stream):
             for _ in range(w):
-                ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+                one_build()
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(k)]
             for e0, e1 in ev:
                 flush.fill_(1.0)
                 e0.record(stream)
-                ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+                one_build()
                 e1.record(stream)
         stream.synchronize()
         return [e0.elapsed_time(e1) for e0, e1 in ev]
@@ -536,7 +595,7 @@ def main():
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_max = float(t.item())
-    value = world * nq / (ms_max * 1e-3)
+    value = nq / (ms_max * 1e-3)
     st = ctx.stats()
 
     # ---- per-launch profile -> dominant kernel roofline ----
@@ -589,7 +648,8 @@ def main():
     # per-class launch times of the mixed build (classes one by one): FP32 and FP64 shares
     pc_mx = profile_classes(torch, lib, ctx, D, flush)
     ctx.set_precision(L.FOCK_PREC_FP64, th)
-    ctx.build_jk_device(D.data_ptr(), G.data_ptr())
+    with torch.cuda.stream(stream):
+        one_build()
     stream.synchronize()
     # energy of one mixed build at the converged density vs the FP64 build: 1/2 sum D (G_mixed - G_fp64)
     de_build = 0.5 * float((D * (Gm - G)).sum().item())
@@ -606,30 +666,49 @@ def main():
     if rmx is not None:
         mixed["abs_energy_error_vs_fp64_eh"] = abs(rmx.total_energy - r64.total_energy)
     # error per ERI of the FP32 kernels: the benzene tensor with every quartet in FP32
-    t64 = F.ElectronTensor.from_basis(atoms, device=local).data
-    t32 = F.ElectronTensor.from_basis(atoms, device=local, precision=L.FOCK_PREC_MIXED, mixed_threshold=1e30).data
-    err = np.abs(t32 - t64)
-    big = np.abs(t64) > 1e-3
-    mixed["fp32_eri_error"] = {"max_abs": float(err.max()), "rms_abs": float(np.sqrt((err ** 2).mean())),
-                               "max_rel_for_abs_above_1e-3": float((err[big] / np.abs(t64[big])).max()),
-                               "integrals": int(t64.size)}
-    del t64, t32, err
+    if rank == 0:
+        t64 = F.ElectronTensor.from_basis(atoms, device=local).data
+        t32 = F.ElectronTensor.from_basis(atoms, device=local, precision=L.FOCK_PREC_MIXED,
+                                          mixed_threshold=1e30).data
+        err = np.abs(t32 - t64)
+        big = np.abs(t64) > 1e-3
+        mixed["fp32_eri_error"] = {"max_abs": float(err.max()), "rms_abs": float(np.sqrt((err ** 2).mean())),
+                                   "max_rel_for_abs_above_1e-3": float((err[big] / np.abs(t64[big])).max()),
+                                   "integrals": int(t64.size)}
+        del t64, t32, err
 
     # ---- e2e through the C ABI with host buffers ----
     Dh = np.ascontiguousarray(r64.density_matrix)
     ctx.set_stream(0)
+
+    def e2e_build():
+        Gh = ctx.build_jk(Dh)
+        if dist:  # the partial G of this rank's shard, summed over the ranks on the device
+            Gt = torch.from_numpy(Gh).cuda()
+            dist.all_reduce(Gt)
+            Gh = Gt.cpu().numpy()
+        return Gh
+
     for _ in range(args.warmup):
-        ctx.build_jk(Dh)
+        e2e_build()
     te = []
     for _ in range(args.steps):
         flush.fill_(1.0)
         torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
         t0 = time.perf_counter()
-        ctx.build_jk(Dh)
+        e2e_build()
         te.append(time.perf_counter() - t0)
     e2e_s = statistics.mean(te)
-    e2e = {"value": world * nq / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * n * 8, "d2h_bytes_per_step": n * n * 8,
-           "ms_per_step": e2e_s * 1e3, "api": "fock_build_jk (host D in, host G out)"}
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": nq / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * n * 8 * (2 if dist else 1),
+           "d2h_bytes_per_step": n * n * 8 * (2 if dist else 1),
+           "ms_per_step": e2e_s * 1e3, "api": "fock_build_jk (host D in, host G out)" +
+           (" + all-reduce of G over the ranks" if dist else "")}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -646,6 +725,7 @@ def main():
         for key, fn in (("batch_512_water_clusters_631g", lambda: batch_workload(torch, F, L, local, flush)),
                         ("water32_631gs", lambda: water32_workload(torch, F, L, local, flush)),
                         ("octane_631g_gradient", lambda: octane_gradient_workload(torch, F, L, local)),
+                        ("shard_balance_water32", lambda: shard_balance_workload(torch, F, L, local, flush)),
                         ("orbital_grid_benzene_homo", lambda: orbital_grid_workload(
                             torch, F, L, local, atoms, r64.coefficient_matrix, r64.n_electrons // 2, opts))):
             try:
@@ -655,9 +735,10 @@ def main():
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+                "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+                "scaling": "strong" if world > 1 else "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": dict(WORKLOAD, parallelism="replicas" if world > 1 else "single"),
+                "config": dict(WORKLOAD, parallelism=parallelism(world)),
                 "clocks": clk, "gpu_launches": launches, "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu,
                 "mixed": mixed, "stats": {k: st[k] for k in ("shell_quartets_fp64", "prim_quartets_fp64",
                                                                "shell_quartets_screened", "launches_per_build")}}

@@ -693,8 +693,8 @@ void fock_options_default(fock_options* o) {
   o->energy_mode = 0;
   o->final_fp64 = 1;
   o->prims_per_slice = -4;        // about 4 primitive quartets per lane
-  o->prims_per_slice_fp32 = -32;
-  o->block_threads = 128;
+  o->prims_per_slice_fp32 = -128;
+  o->block_threads = 64;
   o->persistent = 0;
   o->shard_index = 0;
   o->shard_count = 1;
@@ -1218,7 +1218,7 @@ int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best)
     c->opt.persistent = t.persistent;
   };
   int rc = measure(&cur.ms);
-  const std::vector<int> pps64 = {1, 2, 4, -8, -16, -32}, pps32 = {1, 2, 4, 8, -16, -32, -64}, blk = {64, 128, 256},
+  const std::vector<int> pps64 = {1, 2, 4, -8, -16, -32}, pps32 = {1, 4, -16, -32, -64, -128, -256}, blk = {64, 128, 256},
                          per = {0, 1};
   for (int dim = 0; dim < 4 && rc == FOCK_OK; ++dim) {
     const std::vector<int>& cand = dim == 0 ? pps64 : dim == 1 ? pps32 : dim == 2 ? blk : per;
@@ -1509,10 +1509,22 @@ int fock_gradient(fock_ctx* c, const double* D, const double* W, double* grad) {
     EriArgs a = eri_args(c);
     a.D = c->d_D;
     a.grad = d_grad;
-    for (const Plan& p : c->plans) {
-      e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_GRAD, PREC_FP64, c->stream);
+    // the class launches forked over the side streams, largest first, as in
+    // the Fock build (small d-class launches overlap instead of queueing)
+    const std::vector<int> order = plan_order(c);
+    const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
+    e = cudaEventRecord(c->fork_ev, c->stream);
+    int forked = 0;
+    for (; forked < nside && e == cudaSuccess; ++forked) e = cudaStreamWaitEvent(c->side[forked], c->fork_ev, 0);
+    for (size_t k = 0; k < order.size() && e == cudaSuccess; ++k) {
+      const Plan& p = c->plans[order[k]];
+      e = launch_eri_class(p.la, p.lb, p.lc, p.ld, p.cl, a, MODE_GRAD, PREC_FP64, c->side[k % nside]);
       c->launches++;
-      if (e != cudaSuccess) break;
+    }
+    for (int s = 0; s < forked; ++s) {  // join every side stream that took part, also after an error
+      cudaError_t e2 = cudaEventRecord(c->join_ev[s], c->side[s]);
+      if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(c->stream, c->join_ev[s], 0);
+      if (e == cudaSuccess) e = e2;
     }
   }
   if (e == cudaSuccess) {

@@ -223,62 +223,120 @@ __device__ double prim_nuclear(const int A[3], double a, const int B[3], double 
 // phi' = (A - r)^a e^{-alpha |r - A|^2} functions, converted to the textbook
 // convention by the pair's sign.  The nucleus-centre derivative of V^C is
 // -(d_A + d_B) V^C (translational invariance).  D, W row-major, textbook sign.
-__global__ void one_electron_grad_kernel(const MdBasis B, const MdTables tb, const double* __restrict__ atoms,
-                                         int natom, const int* __restrict__ func_atom, int flags,
-                                         const double* __restrict__ D, const double* __restrict__ W, double* grad) {
+//
+// One warp per function pair (grid-stride over pairs); the lanes take the
+// pair's items: (nucleus c, primitive pair), nucleus-major, and the primitive
+// pairs of S and T as nucleus natom.  A nuclear-attraction item builds its
+// Hermite tables E (indices up to l + 1 on each axis) and R (orders up to
+// L + 1) once and forms all twelve shifted integrals of the three axes and two
+// centres from them.  Gradient contributions gather in a shared-memory copy of
+// the gradient (global memory above kGradSmemAtoms atoms), flushed once per
+// block.
+constexpr int kGradSmemAtoms = 2048;
+constexpr int kGradWarps = 8;
+
+__global__ void __launch_bounds__(kGradWarps * 32) one_electron_grad_kernel(
+    const MdBasis B, const MdTables tb, const double* __restrict__ atoms, int natom, const int* __restrict__ func_atom,
+    int flags, const double* __restrict__ D, const double* __restrict__ W, double* grad) {
+  extern __shared__ double gsm[];
+  const bool smem = natom <= kGradSmemAtoms;
+  double* acc = smem ? gsm : grad;
+  if (smem) {
+    for (int k = threadIdx.x; k < 3 * natom; k += blockDim.x) gsm[k] = 0.0;
+    __syncthreads();
+  }
   const int n = B.nfunc;
   const long long npair = (long long)n * (n + 1) / 2;
-  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (t >= npair) return;
-  int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-  while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
-  while ((long long)i * (i + 1) / 2 > t) --i;
-  const int j = (int)(t - (long long)i * (i + 1) / 2);
-  const MdFunc fa = B.funcs[j], fb = B.funcs[i];  // j <= i
-  const double diff[3] = {fb.c[0] - fa.c[0], fb.c[1] - fa.c[1], fb.c[2] - fa.c[2]};
-  const double sg = fsign(fa) * fsign(fb) * (i == j ? 1.0 : 2.0);
-  const double dij = D[(size_t)i * n + j], wij = W[(size_t)i * n + j];
-  double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
-  for (int c = 0; c < natom; ++c) {
-    double gC[3] = {0, 0, 0};
-    for (int pa = 0; pa < fa.np; ++pa)
-      for (int pb = 0; pb < fb.np; ++pb) {
-        const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
-        const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb] * sg;
-        double P[3];
-        for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / (a + b);
+  const int lane = threadIdx.x & 31;
+  for (long long t = (long long)blockIdx.x * kGradWarps + (threadIdx.x >> 5); t < npair;
+       t += (long long)gridDim.x * kGradWarps) {
+    int i = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long long)(i + 1) * (i + 2) / 2 <= t) ++i;
+    while ((long long)i * (i + 1) / 2 > t) --i;
+    const int j = (int)(t - (long long)i * (i + 1) / 2);
+    const MdFunc fa = B.funcs[j], fb = B.funcs[i];  // j <= i
+    const double diff[3] = {fb.c[0] - fa.c[0], fb.c[1] - fa.c[1], fb.c[2] - fa.c[2]};
+    const double sg = fsign(fa) * fsign(fb) * (i == j ? 1.0 : 2.0);
+    const double dij = D[(size_t)i * n + j], wij = W[(size_t)i * n + j];
+    const int L = fa.ang[0] + fa.ang[1] + fa.ang[2] + fb.ang[0] + fb.ang[1] + fb.ang[2];
+    const int nprim = fa.np * fb.np;
+    const int nitem = nprim * (natom + 1);
+    double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+    for (int it = lane; it < nitem; it += 32) {
+      const int c = it / nprim, pp = it - c * nprim;
+      const int pa = pp / fb.np, pb = pp - pa * fb.np;
+      const double a = B.exps[fa.p0 + pa], b = B.exps[fb.p0 + pb];
+      const double cc = B.coefs[fa.p0 + pa] * B.coefs[fb.p0 + pb] * sg;
+      if (c == natom) {  // overlap and kinetic, once per primitive pair
         for (int x = 0; x < 3; ++x) {
           int Ap[3] = {fa.ang[0], fa.ang[1], fa.ang[2]}, Am[3] = {fa.ang[0], fa.ang[1], fa.ang[2]};
           int Bp[3] = {fb.ang[0], fb.ang[1], fb.ang[2]}, Bm[3] = {fb.ang[0], fb.ang[1], fb.ang[2]};
           Ap[x] += 1; Am[x] -= 1; Bp[x] += 1; Bm[x] -= 1;
-          const double vA = -2.0 * a * prim_nuclear(Ap, a, fb.ang, b, diff, P, atoms + 4 * c, flags, tb) +
-                            (double)fa.ang[x] * prim_nuclear(Am, a, fb.ang, b, diff, P, atoms + 4 * c, flags, tb);
-          const double vB = -2.0 * b * prim_nuclear(fa.ang, a, Bp, b, diff, P, atoms + 4 * c, flags, tb) +
-                            (double)fb.ang[x] * prim_nuclear(fa.ang, a, Bm, b, diff, P, atoms + 4 * c, flags, tb);
-          gA[x] += cc * dij * vA;
-          gB[x] += cc * dij * vB;
-          gC[x] -= cc * dij * (vA + vB);
-          if (c == 0) {  // overlap and kinetic once per pair
-            const double sA = -2.0 * a * prim_overlap(Ap, a, fb.ang, b, diff) +
-                              (double)fa.ang[x] * prim_overlap(Am, a, fb.ang, b, diff);
-            const double sB = -2.0 * b * prim_overlap(fa.ang, a, Bp, b, diff) +
-                              (double)fb.ang[x] * prim_overlap(fa.ang, a, Bm, b, diff);
-            const double tA = -2.0 * a * prim_kinetic(Ap, a, fb.ang, b, diff) +
-                              (double)fa.ang[x] * (fa.ang[x] > 0 ? prim_kinetic(Am, a, fb.ang, b, diff) : 0.0);
-            const double tB = -2.0 * b * prim_kinetic(fa.ang, a, Bp, b, diff) +
-                              (double)fb.ang[x] * (fb.ang[x] > 0 ? prim_kinetic(fa.ang, a, Bm, b, diff) : 0.0);
-            gA[x] += cc * (dij * tA - wij * sA);
-            gB[x] += cc * (dij * tB - wij * sB);
-          }
+          const double sA = -2.0 * a * prim_overlap(Ap, a, fb.ang, b, diff) +
+                            (double)fa.ang[x] * prim_overlap(Am, a, fb.ang, b, diff);
+          const double sB = -2.0 * b * prim_overlap(fa.ang, a, Bp, b, diff) +
+                            (double)fb.ang[x] * prim_overlap(fa.ang, a, Bm, b, diff);
+          const double tA = -2.0 * a * prim_kinetic(Ap, a, fb.ang, b, diff) +
+                            (double)fa.ang[x] * (fa.ang[x] > 0 ? prim_kinetic(Am, a, fb.ang, b, diff) : 0.0);
+          const double tB = -2.0 * b * prim_kinetic(fa.ang, a, Bp, b, diff) +
+                            (double)fb.ang[x] * (fb.ang[x] > 0 ? prim_kinetic(fa.ang, a, Bm, b, diff) : 0.0);
+          gA[x] += cc * (dij * tA - wij * sA);
+          gB[x] += cc * (dij * tB - wij * sB);
         }
+        continue;
       }
-    for (int x = 0; x < 3; ++x)
-      if (gC[x] != 0.0) atomicAdd(grad + 3 * c + x, gC[x]);
+      // nuclear attraction of nucleus c: N(A', B') = -Z 2pi/p sum E E E R(p, C - P)
+      const double p = a + b;
+      double P[3];
+      for (int x = 0; x < 3; ++x) P[x] = (a * fa.c[x] + b * fb.c[x]) / p;
+      ETable<3, 3> E[3];
+      for (int x = 0; x < 3; ++x) etab_build(fa.ang[x] + 1, fb.ang[x] + 1, diff[x], a, b, E[x]);
+      const double* Cz = atoms + 4 * c;
+      const double dcp[3] = {Cz[0] - P[0], Cz[1] - P[1], Cz[2] - P[2]};
+      const double r2 = dcp[0] * dcp[0] + dcp[1] * dcp[1] + dcp[2] * dcp[2];
+      RTable<5> R;
+      rtab_build(L + 1, p, dcp, r2, flags, tb, R);
+      const double zf = -Cz[3] * (2.0 * M_PI) / p;
+      auto nuc = [&](const int* Aq, const int* Bq) -> double {
+        for (int k = 0; k < 3; ++k)
+          if (Aq[k] < 0 || Bq[k] < 0) return 0.0;
+        double sum = 0.0;
+        for (int tt = 0; tt <= Aq[0] + Bq[0]; ++tt)
+          for (int u = 0; u <= Aq[1] + Bq[1]; ++u)
+            for (int v = 0; v <= Aq[2] + Bq[2]; ++v)
+              sum += E[0].e[Aq[0]][Bq[0]][tt] * E[1].e[Aq[1]][Bq[1]][u] * E[2].e[Aq[2]][Bq[2]][v] * R.at(tt, u, v);
+        return zf * sum;
+      };
+      double gC[3];
+      for (int x = 0; x < 3; ++x) {
+        int Ap[3] = {fa.ang[0], fa.ang[1], fa.ang[2]}, Am[3] = {fa.ang[0], fa.ang[1], fa.ang[2]};
+        int Bp[3] = {fb.ang[0], fb.ang[1], fb.ang[2]}, Bm[3] = {fb.ang[0], fb.ang[1], fb.ang[2]};
+        Ap[x] += 1; Am[x] -= 1; Bp[x] += 1; Bm[x] -= 1;
+        const double vA = -2.0 * a * nuc(Ap, fb.ang) + (double)fa.ang[x] * nuc(Am, fb.ang);
+        const double vB = -2.0 * b * nuc(fa.ang, Bp) + (double)fb.ang[x] * nuc(fa.ang, Bm);
+        gA[x] += cc * dij * vA;
+        gB[x] += cc * dij * vB;
+        gC[x] = -cc * dij * (vA + vB);
+      }
+      for (int x = 0; x < 3; ++x) atomicAdd(acc + 3 * c + x, gC[x]);
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int x = 0; x < 3; ++x) {
+        gA[x] += __shfl_down_sync(0xffffffffu, gA[x], o);
+        gB[x] += __shfl_down_sync(0xffffffffu, gB[x], o);
+      }
+    if (lane == 0) {
+      const int atA = func_atom[j], atB = func_atom[i];
+      for (int x = 0; x < 3; ++x) {
+        atomicAdd(acc + 3 * atA + x, gA[x]);
+        atomicAdd(acc + 3 * atB + x, gB[x]);
+      }
+    }
   }
-  const int atA = func_atom[j], atB = func_atom[i];
-  for (int x = 0; x < 3; ++x) {
-    atomicAdd(grad + 3 * atA + x, gA[x]);
-    atomicAdd(grad + 3 * atB + x, gB[x]);
+  if (smem) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < 3 * natom; k += blockDim.x)
+      if (gsm[k] != 0.0) atomicAdd(grad + k, gsm[k]);
   }
 }
 
@@ -286,9 +344,14 @@ cudaError_t md_one_electron_grad(const MdBasis& B, const MdTables& tb, const dou
                                  const int* func_atom, int flags, const double* D, const double* W, double* grad,
                                  cudaStream_t s) {
   const long long np = (long long)B.nfunc * (B.nfunc + 1) / 2;
-  const int thr = 64;
-  one_electron_grad_kernel<<<(unsigned)((np + thr - 1) / thr), thr, 0, s>>>(B, tb, atoms, natom, func_atom, flags, D,
-                                                                           W, grad);
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long want = (np + kGradWarps - 1) / kGradWarps;
+  const long long cap = 4LL * (nsm > 0 ? nsm : 1);
+  const unsigned blocks = (unsigned)(want < cap ? want : cap);
+  const size_t shm = natom <= kGradSmemAtoms ? (size_t)3 * natom * sizeof(double) : 0;
+  one_electron_grad_kernel<<<blocks, kGradWarps * 32, shm, s>>>(B, tb, atoms, natom, func_atom, flags, D, W, grad);
   return cudaGetLastError();
 }
 

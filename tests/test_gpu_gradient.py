@@ -116,9 +116,10 @@ def test_gradient_vs_reference_energy_fd(gpu_lib, oracle_lib):
 
 
 def test_gradient_d_shells_all_components(gpu_lib):
-    """6-31G* (Cartesian d on O): the d-containing classes take the finite-difference
-    derivative kernel, the s/p classes the analytic one; every component of a
-    water dimer against central differences of the SCF energy."""
+    """6-31G* (Cartesian d on O): the d-containing classes take the dual-number
+    derivative kernels ((dd|dd) the finite difference of integrals), the s/p
+    classes the generated analytic one; every component of a water dimer
+    against central differences of the SCF energy."""
     Zs, xyz = M.water_cluster(2, seed=0)
     e0, g = energy_and_gradient("6-31G*", Zs, xyz)
     assert g.shape == (6, 3)
