@@ -43,7 +43,7 @@ UNIT = "quartets/s"
 SCF_GUESS_NAME = "sad"
 BATCH_LEVEL_SHIFT = 0.0  # Eh
 MIXED_CURVE = (1.0, 0.1, 0.01, 1e-3, 1e-4)  # mixed thresholds of the batch's speed / accuracy curve
-BUILD_DRAM_BYTES_NCU = 25.0e6  # bytes per benzene FP64 build under ncu (launch list, 4 builds / 4)
+BUILD_DRAM_BYTES_NCU = 4.7e6  # DRAM bytes per benzene FP64 build under ncu (launch list: 4 builds / 4)
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
             "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
 

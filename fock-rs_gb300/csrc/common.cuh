@@ -48,7 +48,15 @@ struct PairInfo {
   int atom_a, atom_b;  // centres of shells a and b (gradient)
   int mol_off;    // offset of this molecule's n x n block in D, M, G (batches)
   int mol_n;      // basis size of this molecule: row stride of that block
+  int pair0;      // index of the molecule's first shell pair: pairs enumerate
+  int shell0;     // the molecule's shells i (from shell0) with j <= i
 };
+
+// Index of the shell pair {x, y} (shells of the molecule of P) in the pair list.
+__host__ __device__ __forceinline__ int pair_index(const PairInfo& P, int x, int y) {
+  const int hi = (x > y ? x : y) - P.shell0, lo = (x > y ? y : x) - P.shell0;
+  return P.pair0 + hi * (hi + 1) / 2 + lo;
+}
 
 // Primitive pair, double: {p, 1/(2p)}, {K, Px}, {Py, Pz}, {PAx, PAy},
 // {PAz, exponent-sum id as integer bits}, {alpha (exponent of shell a), 0} with
@@ -80,7 +88,9 @@ struct __align__(16) ExpPair64 {
 // packed densely: lane t of the launch takes row r with
 // row_off[r] <= t < row_off[r+1] (row_off: prefix sum of row_cnt * row_slices),
 // slice (t - row_off[r]) / row_cnt[r] and the ket at the remainder, so every
-// warp is full except the launch's last.  Schwarz mode: bra_list holds nrows
+// warp is full except the launch's last.  With ket slices (row_kslices), a
+// slice s of row r covers bra slice s / k and ket slice s % k of the
+// primitive pairs, k = row_kslices[r].  Schwarz mode: bra_list holds nrows
 // pairs, one per thread.
 struct ClassLaunch {
   const int* bra_list;
@@ -88,6 +98,7 @@ struct ClassLaunch {
   const int* row_beg;
   const int* row_cnt;
   const int* row_slices;
+  const int* row_kslices;        // ket primitive slices per row (nullptr: 1); row_slices counts both
   const long long* row_off;
   int nrows;
   long long nlanes;
@@ -115,6 +126,7 @@ struct EriArgs {
   int nxp;
   const double* D;        // density, nbf x nbf row-major (textbook sign convention)
   const float* D32;       // float copy for the FP32 digestion
+  const float* pair_dmax; // max |D32| over each shell pair's block (density-weighted split)
   double* M;              // accumulator: G = M + M^T
   double* tensor;         // MODE_TENSOR output, nbf^4
   float* schwarz;         // MODE_SCHWARZ output per pair

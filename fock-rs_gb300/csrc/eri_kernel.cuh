@@ -123,10 +123,12 @@ __device__ __forceinline__ float pair_ab<float>(const PairInfo& P, int i) { retu
 __device__ __forceinline__ double to_f64(double x) { return x; }
 __device__ __forceinline__ double to_f64(float x) { return f2d_exact(x); }
 
-// Lane t of a launch -> (bra pair, ket pair, bra slice); see ClassLaunch.
-// Also returns the row (*row) and the ket's index within it (*kloc).
+// Lane t of a launch -> (bra pair, ket pair, bra slice of nslice); see
+// ClassLaunch.  Also returns the row (*row), the ket's index within it
+// (*kloc) and the ket slice (*ks of *nks; 0 of 1 without ket slices).
 __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, int& bra, int& ket, int& slice,
-                                            int& nslice, int* row = nullptr, int* kloc = nullptr) {
+                                            int& nslice, int* row = nullptr, int* kloc = nullptr,
+                                            int* ks = nullptr, int* nks = nullptr) {
   int lo = 0, hi = cl.nrows - 1;
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -137,6 +139,16 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
   nslice = __ldg(cl.row_slices + lo);
   slice = (int)(local / cnt);
   const int k = (int)(local - (long long)slice * cnt);
+  const int nk = cl.row_kslices ? __ldg(cl.row_kslices + lo) : 1;
+  if (nk > 1) {
+    const int s = slice;
+    slice = s / nk;
+    nslice /= nk;
+    if (ks) *ks = s - slice * nk;
+  } else if (ks) {
+    *ks = 0;
+  }
+  if (nks) *nks = nk;
   bra = __ldg(cl.bra_list + lo);
   ket = __ldg(cl.ket_list + __ldg(cl.row_beg + lo) + k);
   if (row) *row = lo;
@@ -144,22 +156,17 @@ __device__ __forceinline__ void decode_lane(const ClassLaunch& cl, long long t, 
 }
 
 // max |D| over the six density blocks a quartet is contracted with (ab, cd,
-// ac, ad, bc, bd), from the float density copy: the same value in the FP64
-// and the FP32 launches of a class.
-template <class C>
-__device__ __forceinline__ float quartet_dmax(const EriArgs& a, size_t mo, int ld, int fa, int fb, int fc, int fd) {
-  float w = 0.0f;
-  auto blk = [&](int f0, int n0, int f1, int n1) {
-    for (int i = 0; i < n0; ++i)
-      for (int j = 0; j < n1; ++j) w = fmaxf(w, fabsf(__ldg(a.D32 + mo + (size_t)(f0 + i) * ld + f1 + j)));
-  };
-  blk(fa, C::NA, fb, C::NB);
-  blk(fc, C::NC, fd, C::ND);
-  blk(fa, C::NA, fc, C::NC);
-  blk(fa, C::NA, fd, C::ND);
-  blk(fb, C::NB, fc, C::NC);
-  blk(fb, C::NB, fd, C::ND);
-  return w;
+// ac, ad, bc, bd), from the per-build table of shell-pair block maxima of the
+// float density copy: the same value in the FP64 and the FP32 launches of a
+// class.
+__device__ __forceinline__ float quartet_dmax(const EriArgs& a, int bra, int ket, const PairInfo& Pb,
+                                              const PairInfo& Pk) {
+  const float* t = a.pair_dmax;
+  float w = fmaxf(__ldg(t + bra), __ldg(t + ket));
+  w = fmaxf(w, __ldg(t + pair_index(Pb, Pb.sa, Pk.sa)));
+  w = fmaxf(w, __ldg(t + pair_index(Pb, Pb.sa, Pk.sb)));
+  w = fmaxf(w, __ldg(t + pair_index(Pb, Pb.sb, Pk.sa)));
+  return fmaxf(w, __ldg(t + pair_index(Pb, Pb.sb, Pk.sb)));
 }
 
 // The work of lane t of a launch (one contracted quartet, one bra slice).
@@ -168,7 +175,7 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   constexpr int NA = C::NA, NB = C::NB, NC = C::NC, ND = C::ND, NE = C::NE, NF = C::NF, L = C::L;
   int bra, ket;
   bool active;
-  int slice = 0, nslice = 1;
+  int slice = 0, nslice = 1, kslice = 0, nkslice = 1;
   if (MODE == MODE_SCHWARZ) {
     active = t < cl.nrows;
     bra = ket = cl.bra_list[active ? t : 0];
@@ -179,12 +186,12 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
     active = t < cl.nlanes;
     if (active) {
       int row, kloc;
-      decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc);
+      decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc, &kslice, &nkslice);
       if (cl.row_split && kloc < __ldg(cl.row_split + row)) {
         // density-weighted precision split: this launch keeps its side of the bound
         const PairInfo& Pb = a.pairs[bra];
         const PairInfo& Pk = a.pairs[ket];
-        const float w = quartet_dmax<C>(a, (size_t)Pb.mol_off, Pb.mol_n, Pb.fa, Pb.fb, Pk.fa, Pk.fb);
+        const float w = quartet_dmax(a, bra, ket, Pb, Pk);
         const bool heavy = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), w) >= cl.wthr;
         active = heavy == (sizeof(R) == sizeof(double));
       }
@@ -204,13 +211,16 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   // this warp's slice of the bra primitive pairs
   const int ib0 = (int)(((long long)slice * Pb.nprim) / nslice);
   const int ib1 = (int)(((long long)(slice + 1) * Pb.nprim) / nslice);
-  const int nkp = active ? Pk.nprim : 0;
-  const int bp0 = Pb.prim_off, kp0 = Pk.prim_off;
+  // and of the ket primitive pairs (ket slices: the FP64 side of a split)
+  const int ik0 = (int)(((long long)kslice * Pk.nprim) / nkslice);
+  const int ik1 = active ? (int)(((long long)(kslice + 1) * Pk.nprim) / nkslice) : ik0;
+  const int nkp = ik1 - ik0;
+  const int bp0 = Pb.prim_off, kp0 = Pk.prim_off + ik0;
   if (MODE == MODE_JK && cl.counters) {
     // work actually computed (the split is decided per build): one atomic per warp
     const unsigned m = __activemask();
     const unsigned pq = __reduce_add_sync(m, (unsigned)((ib1 - ib0) * nkp));
-    const unsigned q = __reduce_add_sync(m, (active && slice == 0) ? 1u : 0u);
+    const unsigned q = __reduce_add_sync(m, (active && slice == 0 && kslice == 0) ? 1u : 0u);
     if ((threadIdx.x & 31) == __ffs(m) - 1) {
       atomicAdd(cl.counters, (unsigned long long)q);
       atomicAdd(cl.counters + 1, (unsigned long long)pq);

@@ -219,6 +219,7 @@ struct fock_ctx {
   // density / Fock buffers
   double *d_D = nullptr, *d_M = nullptr, *d_G = nullptr;
   float* d_D32 = nullptr;
+  float* d_pair_dmax = nullptr;  // per build: max |D32| of each shell pair's block (mixed split)
   // plans
   std::vector<Plan> plans;
   int* d_plan_int = nullptr;
@@ -272,6 +273,7 @@ EriArgs eri_args(fock_ctx* c) {
   a.M = c->d_M;
   a.tensor = nullptr;
   a.schwarz = c->d_schwarz;
+  a.pair_dmax = c->d_pair_dmax;
   a.grad = nullptr;
   a.nbf = c->nbf;
   return a;
@@ -462,13 +464,13 @@ int build_plan(fock_ctx* c, bool for_tensor) {
 
   std::vector<int> ints;
   std::vector<long long> lls;
-  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, split, off; };
+  struct Pending { Plan p; size_t bra, ket, beg, cnt, sl, ks, split, off; };
   std::vector<Pending> pend;
   fock_stats st{};
   st.shell_pairs = (long long)c->hpairs.size();
   st.prim_pairs = c->nprim_pairs;
   st.function_quartets_unique = cat.function_quartets_unique;
-  std::vector<int> rbra, rbeg, rcnt, kets, rsl, rsplit;
+  std::vector<int> rbra, rbeg, rcnt, kets, rsl, rks, rsplit;
   // one launch per class and precision: the catalog's groups of a class (one
   // per ket primitive-pair count, adjacent in the catalog) are concatenated,
   // so a warp mixes trip counts only where two groups meet
@@ -534,16 +536,30 @@ int build_plan(fock_ctx* c, bool for_tensor) {
       // (bra primitive pairs per lane = ceil(-pps / ket primitive pairs of the row))
       const int pps = for_tensor ? (1 << 30)
                       : (P.p.prec == PREC_FP32 ? c->opt.prims_per_slice_fp32 : c->opt.prims_per_slice);
+      // The FP64 launch of a density-weighted split keeps few quartets, and
+      // they are the heaviest (core-core pairs, up to 36 x 36 primitive
+      // pairs): its rows also split the ket primitive pairs over lanes
+      // (ket slices), so that these quartets spread over the GPU instead of
+      // running a long primitive loop on few lanes.
+      const bool kslicing = !for_tensor && pps < 0 && P.p.prec == PREC_FP64 && mixed && density;
       rsl.resize(rbra.size());
+      rks.assign(rbra.size(), 1);
       for (size_t r = 0; r < rbra.size(); ++r) {
         int per = std::max(1, pps);
         if (pps < 0) {
           const int nk = std::max(1, c->hpairs[kets[rbeg[r]]].nprim);
-          per = std::max(1, (-pps + nk - 1) / nk);
+          if (kslicing && nk > -pps) {
+            per = 1;
+            rks[r] = (nk + (-pps) - 1) / (-pps);
+          } else {
+            per = std::max(1, (-pps + nk - 1) / nk);
+          }
         }
-        rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + per - 1) / per);
+        rsl[r] = std::max(1, (c->hpairs[rbra[r]].nprim + per - 1) / per) * rks[r];
       }
       ints.insert(ints.end(), rsl.begin(), rsl.end());
+      P.ks = ints.size();
+      if (kslicing) ints.insert(ints.end(), rks.begin(), rks.end());
       P.split = ints.size();
       ints.insert(ints.end(), rsplit.begin(), rsplit.end());
       P.off = lls.size();
@@ -583,6 +599,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.row_beg = c->d_plan_int + P.beg;
     P.p.cl.row_cnt = c->d_plan_int + P.cnt;
     P.p.cl.row_slices = c->d_plan_int + P.sl;
+    P.p.cl.row_kslices = P.ks < P.split ? c->d_plan_int + P.ks : nullptr;
     P.p.cl.row_off = c->d_plan_ll + P.off;
     P.p.cl.block = c->opt.block_threads;
     P.p.cl.persist_blocks = (!for_tensor && c->opt.persistent) ? -1 : 0;
@@ -765,7 +782,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
   dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64);
-  dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32);
+  dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32); dfree(c->d_pair_dmax);
   dfree(c->d_plan_int); dfree(c->d_plan_ll);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
   dfree(c->d_mol_off); dfree(c->d_mol_n);
@@ -873,6 +890,12 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   std::vector<PrimPair64> p64;
   std::vector<PrimPair32> p32;
   const double kpref = std::sqrt(2.0) * std::pow(M_PI, 1.25);
+  // first pair of each molecule: pairs enumerate shells i with j <= i per molecule
+  std::vector<int> mol_pair0(nmol, 0);
+  for (int m = 1; m < nmol; ++m) {
+    const long long ns = c->mol_shell0[m] - c->mol_shell0[m - 1];
+    mol_pair0[m] = mol_pair0[m - 1] + (int)(ns * (ns + 1) / 2);
+  }
   for (int i = 0; i < nshell; ++i)
     for (int j = c->mol_shell0[c->shells[i].mol]; j <= i; ++j) {
       int a = i, b = j;
@@ -884,6 +907,8 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       P.atom_a = A.atom; P.atom_b = B.atom;
       P.mol_off = (int)c->mol_off[A.mol];
       P.mol_n = c->mol_nbf[A.mol];
+      P.pair0 = mol_pair0[A.mol];
+      P.shell0 = c->mol_shell0[A.mol];
       P.cls = pair_class(A.l, B.l);
       for (int k = 0; k < 3; ++k) {
         P.AB[k] = A.c[k] - B.c[k];
@@ -959,7 +984,8 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
       (rc = map_cuda(dalloc(&c->d_ref_lut, g_ref_lut.size()))) ||
       (rc = map_cuda(dalloc(&c->d_schwarz, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_D, nn))) || (rc = map_cuda(dalloc(&c->d_M, nn))) ||
-      (rc = map_cuda(dalloc(&c->d_G, nn))) || (rc = map_cuda(dalloc(&c->d_D32, nn))))
+      (rc = map_cuda(dalloc(&c->d_G, nn))) || (rc = map_cuda(dalloc(&c->d_D32, nn))) ||
+      (rc = map_cuda(dalloc(&c->d_pair_dmax, npairs))))
     return fail(rc);
   if ((rc = map_cuda(cudaMemcpy(c->d_pairs, c->hpairs.data(), npairs * sizeof(PairInfo), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_prim64, p64.data(), p64.size() * sizeof(PrimPair64), cudaMemcpyHostToDevice))) ||
@@ -1068,6 +1094,10 @@ static cudaError_t issue_jk_build(fock_ctx* c, cudaStream_t cs, int* kernels) {
   const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
   cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
   if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); (*kernels)++; }
+  if (e == cudaSuccess && c->split_counts) {
+    e = k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), c->d_D32, c->d_pair_dmax, cs);
+    (*kernels)++;
+  }
   if (e == cudaSuccess && (c->opt.persistent || c->split_counts))
     e = cudaMemsetAsync(c->d_plan_ll + c->queue_base, 0, counter_elems(c) * sizeof(long long), cs);
   if (e == cudaSuccess) e = cudaEventRecord(c->fork_ev, cs);
@@ -1141,6 +1171,10 @@ int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, dou
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
   if (need32) {
     CK(k_to_float(D_dev, D32, (int)nn, cs));
+    c->launches++;
+  }
+  if (c->split_counts) {
+    CK(k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), D32, c->d_pair_dmax, cs));
     c->launches++;
   }
   const std::vector<int> order = plan_order(c);
@@ -1268,6 +1302,10 @@ int fock_profile_build(fock_ctx* c, const double* D_dev, fock_launch_profile* ou
   a.D = D_dev;
   CK(k_to_float(D_dev, c->d_D32, (int)nn, c->stream));
   c->launches++;
+  if (c->split_counts) {
+    CK(k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), c->d_D32, c->d_pair_dmax, c->stream));
+    c->launches++;
+  }
   const int np = (int)c->plans.size();
   std::vector<cudaEvent_t> ev(2 * (size_t)np);
   for (auto& e : ev) CK(cudaEventCreate(&e));

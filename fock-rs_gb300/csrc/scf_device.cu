@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include "common.cuh"
 #include "scf_device.cuh"
 
 namespace fockgb {
@@ -258,10 +259,37 @@ cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s) {
   to_float_kernel<<<blocks_for(nn, 256), 256, 0, s>>>(a, b, nn);
   return cudaGetLastError();
 }
+
+// max |D32| over the block of each shell pair (rows of shell a, columns of
+// shell b, in the pair's molecule block), one thread per pair: the density
+// factor of the density-weighted precision split, once per build instead of
+// once per candidate lane and block.
+__global__ void pair_dmax_kernel(const PairInfo* __restrict__ pairs, int npairs, const float* __restrict__ D32,
+                                 float* out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npairs) return;
+  const PairInfo& P = pairs[p];
+  const int cls = P.cls;
+  int la = 0;
+  while ((la + 1) * (la + 2) / 2 <= cls) ++la;
+  const int lb = cls - la * (la + 1) / 2;
+  const int na = (la + 1) * (la + 2) / 2, nb = (lb + 1) * (lb + 2) / 2;
+  const float* blk = D32 + P.mol_off;
+  float w = 0.0f;
+  for (int i = 0; i < na; ++i)
+    for (int j = 0; j < nb; ++j) w = fmaxf(w, fabsf(blk[(size_t)(P.fa + i) * P.mol_n + P.fb + j]));
+  out[p] = w;
+}
+cudaError_t k_pair_dmax(const PairInfo* pairs, int npairs, const float* D32, float* out, cudaStream_t s) {
+  if (npairs <= 0) return cudaSuccess;
+  pair_dmax_kernel<<<blocks_for(npairs, 256), 256, 0, s>>>(pairs, npairs, D32, out);
+  return cudaGetLastError();
+}
 // Loads the code of the helper kernels of a Fock build (see MODE_PRELOAD).
 cudaError_t k_preload_build_kernels() {
   cudaFuncAttributes fa;
   cudaError_t e = cudaFuncGetAttributes(&fa, symmetrize_kernel);
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, pair_dmax_kernel);
   return e == cudaSuccess ? cudaFuncGetAttributes(&fa, to_float_kernel) : e;
 }
 cudaError_t k_guess(const double* S, const double* H, double* F, int n, int gwh, cudaStream_t s) {

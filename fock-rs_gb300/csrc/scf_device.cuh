@@ -14,6 +14,9 @@ cudaError_t k_symmetrize(const double* M, double* G, int n, cudaStream_t s);
 cudaError_t k_symmetrize_blocks(const double* M, double* G, const long long* off, const int* n, int nmol,
                                 long long total, cudaStream_t s);
 cudaError_t k_to_float(const double* a, float* b, int nn, cudaStream_t s);
+struct PairInfo;
+// out[p] = max |D32| over shell pair p's block (density-weighted precision split)
+cudaError_t k_pair_dmax(const PairInfo* pairs, int npairs, const float* D32, float* out, cudaStream_t s);
 cudaError_t k_preload_build_kernels();
 cudaError_t k_guess(const double* S, const double* H, double* F, int n, int gwh, cudaStream_t s);
 cudaError_t k_scale_cols(const double* U, const double* w, double* W, int n, cudaStream_t s);
