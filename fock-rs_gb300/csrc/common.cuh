@@ -24,7 +24,10 @@ constexpr int kBoysTaylor = 7;
 constexpr int kBoysMaxM = 12;           // orders with a Taylor table
 // FP32 table: 16-byte rows of the first four coefficients (cubic Taylor
 // polynomial, truncation (1/64)^4/4! < 3e-9 relative), half the footprint of
-// the FP64 rows so that the order a class reads stays cache-resident
+// the FP64 rows so that the order a class reads stays cache-resident (a
+// coarser 6-term table of 8 KB per order, measured, made the FP32 launches of
+// L <= 2 slower: the second load and the longer polynomial cost more than the
+// L1 misses they save)
 constexpr int kBoysTerms32 = 4;
 constexpr double kBoysTmax = 64.0;
 constexpr float kBoysTmaxF = 64.0f;
@@ -205,6 +208,16 @@ __device__ __forceinline__ double boys_taylor_row(const double* __restrict__ row
   return f;
 }
 
+// T_i = i / kBoysPerUnit as a double built from its bits with integer
+// operations (i < 2^12, so the significand fits the high word): no FP64-pipe
+// conversion of i.
+__device__ __forceinline__ double grid_point(int i) {
+  static_assert(kBoysPerUnit == 32 && kBoysPts <= 4096, "grid_point assumes T_i = i / 32, i < 2^12");
+  const int e = 31 - __clz(i | 1);  // floor(log2 i) for i > 0
+  const int hi = ((e + 1023 - 5) << 20) | ((i << (20 - e)) & 0xfffff);
+  return i ? __hiloint2double(hi, 0) : 0.0;
+}
+
 // Orders L up to FOCK_BOYS_ROWS_LMAX read one Taylor row per order; higher
 // orders read the row of F_L only and recur downwards with e^{-T}.
 #ifndef FOCK_BOYS_ROWS_LMAX
@@ -219,7 +232,7 @@ __device__ __forceinline__ void boys_scaled(double T, double pref, const double*
   if (Tf < (float)kBoysTmax) {
     int i = __float2int_rn(Tf * (float)kBoysPerUnit);
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
-    const double d = fma((double)i, -1.0 / kBoysPerUnit, T);
+    const double d = T - grid_point(i);
     double ex;
     if (L <= FOCK_BOYS_ROWS_LMAX) {
 #pragma unroll
