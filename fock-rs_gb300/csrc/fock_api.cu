@@ -23,8 +23,8 @@
 #include <cstring>
 #include <mutex>
 #include <numeric>
-#include <string>
 #include <map>
+#include <string>
 #include <vector>
 
 #include "../../include/fock_gb300.h"
@@ -74,6 +74,17 @@ constexpr int kTabOrders = kBoysMaxM + kBoysTaylor;  // F_0 .. F_{M+6}
 std::once_flag g_tab_once;
 std::vector<double> g_boys64, g_ref_lut;
 std::vector<float> g_boys32;
+
+// The Boys tables on a device, shared by every context of the process
+// (read-only, 2.1 MB): uploaded by the first context created on the device
+// and kept until the process exits.
+struct DeviceTables {
+  double* boys64 = nullptr;
+  float* boys32 = nullptr;
+  double* ref_lut = nullptr;
+};
+std::mutex g_devtab_mu;
+std::map<int, DeviceTables> g_devtab;
 
 long double boys_series_ld(int n, long double T) {
   long double term = 1.0L / (2 * n + 1), sum = term;
@@ -626,10 +637,13 @@ int compute_schwarz(fock_ctx* c) {
   std::vector<int> all;
   for (auto& v : cls) all.insert(all.end(), v.begin(), v.end());
   CK(cudaMemcpy(d_list, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice));
-  CK(cudaMemset(c->d_schwarz, 0, npairs * sizeof(float)));
+  CK(cudaMemsetAsync(c->d_schwarz, 0, npairs * sizeof(float), c->stream));  // ordered before the fork
   EriArgs a = eri_args(c);
   size_t off = 0;
-  for (int X = 0; X < kNumPairClasses; ++X) {
+  // the pair classes' launches are independent: one side stream each
+  cudaError_t e = cudaEventRecord(c->fork_ev, c->stream);
+  int forked = 0;
+  for (int X = 0; X < kNumPairClasses && e == cudaSuccess; ++X) {
     if (cls[X].empty()) continue;
     int la = 0, lb = 0;
     for (int x = 0; x <= kMaxL; ++x)
@@ -638,13 +652,25 @@ int compute_schwarz(fock_ctx* c) {
     ClassLaunch cl{};
     cl.bra_list = d_list + off;
     cl.nrows = (int)cls[X].size();
-    cudaError_t e = launch_eri_class(la, lb, la, lb, cl, a, MODE_SCHWARZ, PREC_FP64, c->stream);
+    cudaStream_t ss = c->side[forked % kForkStreams];
+    if (forked < kForkStreams) e = cudaStreamWaitEvent(ss, c->fork_ev, 0);
+    ++forked;
+    if (e == cudaSuccess) e = launch_eri_class(la, lb, la, lb, cl, a, MODE_SCHWARZ, PREC_FP64, ss);
     c->launches++;
-    if (e != cudaSuccess) { cudaFree(d_list); return map_cuda(e); }
     off += cls[X].size();
   }
+  for (int k = 0; k < std::min(forked, kForkStreams); ++k) {  // join, also after an error
+    cudaError_t e2 = cudaEventRecord(c->join_ev[k], c->side[k]);
+    if (e2 == cudaSuccess) e2 = cudaStreamWaitEvent(c->stream, c->join_ev[k], 0);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d_list);
+    return map_cuda(e);
+  }
   c->Q.assign(npairs, 0.0f);
-  cudaError_t e = cudaMemcpyAsync(c->Q.data(), c->d_schwarz, npairs * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+  e = cudaMemcpyAsync(c->Q.data(), c->d_schwarz, npairs * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   cudaFree(d_list);
   CK(e);
@@ -781,7 +807,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   cudaSetDevice(c->device);
   if (c->own_stream) cudaStreamSynchronize(c->own_stream);
   dfree(c->d_pairs); dfree(c->d_prim64); dfree(c->d_prim32);
-  dfree(c->d_boys64); dfree(c->d_ref_lut); dfree(c->d_boys32); dfree(c->d_xp64);
+  dfree(c->d_xp64);  // the Boys tables belong to the device (g_devtab)
   dfree(c->d_schwarz); dfree(c->d_D); dfree(c->d_M); dfree(c->d_G); dfree(c->d_D32); dfree(c->d_pair_dmax);
   dfree(c->d_plan_int); dfree(c->d_plan_ll);
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
@@ -839,6 +865,19 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   CK(cudaSetDevice(o.device));
   std::call_once(g_tab_once, build_tables);
 
+  // FOCK_GB300_TRACE=1: host wall time of the set-up phases on stderr
+  const bool trace = std::getenv("FOCK_GB300_TRACE") != nullptr;
+  auto t_last = std::chrono::steady_clock::now();
+  std::string trace_line;
+  auto stamp = [&](const char* phase) {
+    if (!trace) return;
+    cudaDeviceSynchronize();
+    const auto t = std::chrono::steady_clock::now();
+    char buf[96];
+    std::snprintf(buf, sizeof(buf), " %s %.2f ms", phase, 1e3 * std::chrono::duration<double>(t - t_last).count());
+    trace_line += buf;
+    t_last = t;
+  };
   fock_ctx* c = new fock_ctx();
   c->opt = o;
   c->device = o.device;
@@ -886,6 +925,7 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
         cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
       return fail(FOCK_ERR_CUDA);
 
+  stamp("streams");
   // ---- shell pairs and primitive pairs ----
   std::vector<PrimPair64> p64;
   std::vector<PrimPair32> p32;
@@ -961,16 +1001,18 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
     std::memcpy(&idf, &idi, sizeof(idf));
     p32[k].v[2].y = idf;
   }
+  // in double: each entry within about one ulp (long double is a software
+  // quad type on Arm hosts, where this table took milliseconds per context)
   std::vector<ExpPair64> xp64((size_t)c->nxp * c->nxp);
   for (int i = 0; i < c->nxp; ++i)
     for (int j = 0; j < c->nxp; ++j) {
-      const long double p = psum[i], q = psum[j], s = p + q;
+      const double p = psum[i], q = psum[j], s = p + q;
       ExpPair64& e = xp64[(size_t)i * c->nxp + j];
-      e.rs = (double)(1.0L / sqrtl(s));
-      e.o2pq = (double)(0.5L / s);
-      e.rp = (double)(q / s);
-      e.rq = (double)(p / s);
-      e.rho = (double)(p * q / s);
+      e.rs = 1.0 / std::sqrt(s);
+      e.o2pq = 0.5 / s;
+      e.rp = q / s;
+      e.rq = p / s;
+      e.rho = p * (q / s);
       e.pad = 0.0;
     }
   const int npairs = (int)c->hpairs.size();
@@ -978,10 +1020,7 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   if ((rc = map_cuda(dalloc(&c->d_pairs, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_prim64, p64.size()))) ||
       (rc = map_cuda(dalloc(&c->d_prim32, p32.size()))) ||
-      (rc = map_cuda(dalloc(&c->d_boys64, g_boys64.size()))) ||
-      (rc = map_cuda(dalloc(&c->d_boys32, g_boys32.size()))) ||
       (rc = map_cuda(dalloc(&c->d_xp64, xp64.size()))) ||
-      (rc = map_cuda(dalloc(&c->d_ref_lut, g_ref_lut.size()))) ||
       (rc = map_cuda(dalloc(&c->d_schwarz, npairs))) ||
       (rc = map_cuda(dalloc(&c->d_D, nn))) || (rc = map_cuda(dalloc(&c->d_M, nn))) ||
       (rc = map_cuda(dalloc(&c->d_G, nn))) || (rc = map_cuda(dalloc(&c->d_D32, nn))) ||
@@ -990,11 +1029,28 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
   if ((rc = map_cuda(cudaMemcpy(c->d_pairs, c->hpairs.data(), npairs * sizeof(PairInfo), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_prim64, p64.data(), p64.size() * sizeof(PrimPair64), cudaMemcpyHostToDevice))) ||
       (rc = map_cuda(cudaMemcpy(c->d_prim32, p32.data(), p32.size() * sizeof(PrimPair32), cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_boys64, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_boys32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_xp64, xp64.data(), xp64.size() * sizeof(ExpPair64), cudaMemcpyHostToDevice))) ||
-      (rc = map_cuda(cudaMemcpy(c->d_ref_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice))))
+      (rc = map_cuda(cudaMemcpy(c->d_xp64, xp64.data(), xp64.size() * sizeof(ExpPair64), cudaMemcpyHostToDevice))))
     return fail(rc);
+  {  // the device's shared Boys tables (uploaded by the first context on the device)
+    std::lock_guard<std::mutex> lock(g_devtab_mu);
+    DeviceTables& t = g_devtab[o.device];
+    if (!t.boys64) {
+      DeviceTables n;
+      if ((rc = map_cuda(dalloc(&n.boys64, g_boys64.size()))) ||
+          (rc = map_cuda(dalloc(&n.boys32, g_boys32.size()))) ||
+          (rc = map_cuda(dalloc(&n.ref_lut, g_ref_lut.size()))) ||
+          (rc = map_cuda(cudaMemcpy(n.boys64, g_boys64.data(), g_boys64.size() * 8, cudaMemcpyHostToDevice))) ||
+          (rc = map_cuda(cudaMemcpy(n.boys32, g_boys32.data(), g_boys32.size() * 4, cudaMemcpyHostToDevice))) ||
+          (rc = map_cuda(cudaMemcpy(n.ref_lut, g_ref_lut.data(), g_ref_lut.size() * 8, cudaMemcpyHostToDevice)))) {
+        dfree(n.boys64); dfree(n.boys32); dfree(n.ref_lut);
+        return fail(rc);
+      }
+      t = n;
+    }
+    c->d_boys64 = t.boys64;
+    c->d_boys32 = t.boys32;
+    c->d_ref_lut = t.ref_lut;
+  }
 
   // ---- per-function MD basis (one-electron integrals, reference-compatible tensor) ----
   {
@@ -1044,9 +1100,14 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
         (rc = map_cuda(cudaMemcpy(c->d_mol_n, mn.data(), mn.size() * sizeof(int), cudaMemcpyHostToDevice))))
       return fail(rc);
   }
+  stamp("pairs+tables");
   if ((rc = compute_schwarz(c)) != FOCK_OK) return fail(rc);
+  stamp("schwarz");
   if ((rc = build_plan(c, false)) != FOCK_OK) return fail(rc);
+  stamp("plan");
   if (nmol == 1 && (rc = fockgb_noalloc_setup(c)) != FOCK_OK) return fail(rc);
+  stamp("preload");
+  if (trace) std::fprintf(stderr, "fock_ctx_create trace: n %d, %d shells:%s\n", c->nbf, nshell, trace_line.c_str());
   *out = c;
   return FOCK_OK;
 }
@@ -1820,7 +1881,8 @@ int atom_density(int Z, const std::vector<fock_shell>& shells, int device, std::
       F[i] = H[i] + G[i];
       e += 0.5 * D[i] * (H[i] + F[i]);
     }
-    if (it > 0 && dmax < 1e-7 && std::fabs(e - e_prev) < 1e-9) break;
+    // a start needs no tight convergence: the molecular SCF takes it from here
+    if (it > 0 && dmax < 1e-5 && std::fabs(e - e_prev) < 1e-7) break;
     e_prev = e;
   }
   fock_ctx_destroy(ac);
@@ -1833,11 +1895,13 @@ int atom_density(int Z, const std::vector<fock_shell>& shells, int device, std::
 // mol_off (textbook sign convention, symmetric).
 int sad_density(fock_ctx* c, std::vector<double>& Dall) {
   Dall.assign((size_t)c->total_elems, 0.0);
-  // shells of every atom, in context order; atoms with equal element and
-  // shells share one atomic calculation
+  // shells of every atom, in context order
   std::vector<std::vector<int>> atom_shells(c->natom);
   for (int s = 0; s < (int)c->shells.size(); ++s) atom_shells[c->shells[s].atom].push_back(s);
-  std::map<std::vector<double>, std::vector<double>> cache;
+  // atoms of the same element and shells share one calculation, also across
+  // contexts of the process (repeated SCFs: finite differences, batches)
+  static std::mutex cache_mu;
+  static std::map<std::vector<double>, std::vector<double>> cache;
   for (int a = 0; a < c->natom; ++a) {
     const std::vector<int>& sl = atom_shells[a];
     if (sl.empty()) continue;
@@ -1857,14 +1921,18 @@ int sad_density(fock_ctx* c, std::vector<double>& Dall) {
       const HostShell& h = c->shells[sl[q]];
       fs.push_back(fock_shell{h.l, h.nprim, 0, h.exps.data(), raw[q].data()});
     }
-    auto it = cache.find(key);
-    if (it == cache.end()) {
-      std::vector<double> Da;
+    std::vector<double> Da;
+    {
+      std::lock_guard<std::mutex> lock(cache_mu);
+      auto it = cache.find(key);
+      if (it != cache.end()) Da = it->second;
+    }
+    if (Da.empty()) {
       int rc = atom_density(c->atoms[a].Z, fs, c->device, Da);
       if (rc != FOCK_OK) return rc;
-      it = cache.emplace(key, std::move(Da)).first;
+      std::lock_guard<std::mutex> lock(cache_mu);
+      cache.emplace(key, Da);
     }
-    const std::vector<double>& Da = it->second;
     // local function index -> index within the molecule
     std::vector<int> fmap;
     for (int s : sl)
