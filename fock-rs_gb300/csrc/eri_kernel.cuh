@@ -30,6 +30,12 @@ constexpr int kEriMaxThreads = 256;
 #define FOCK_KET_UNROLL 2
 #endif
 constexpr int kKetUnroll = FOCK_KET_UNROLL;
+// FP32 lanes: no unroll (measured: benzene mixed build 0.163 / 0.175 /
+// 0.218 ms with 1 / 2 / 4; (H2O)32 16.6 / 17.1 / 17.2 ms)
+#ifndef FOCK_KET_UNROLL32
+#define FOCK_KET_UNROLL32 1
+#endif
+constexpr int kKetUnroll32 = FOCK_KET_UNROLL32;
 #ifndef FOCK_MINBLOCKS
 #define FOCK_MINBLOCKS 1
 #endif
@@ -248,7 +254,7 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
     } else {
       kp.load(a, kp0 + ik);
     }
-#pragma unroll kKetUnroll
+#pragma unroll(sizeof(R) == sizeof(float) ? kKetUnroll32 : kKetUnroll)
     for (int ib = ib0; ib < ib1; ++ib) {
       PrimLoad<R> bp;
       bp.load(a, bp0 + ib);
