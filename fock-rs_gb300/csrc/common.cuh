@@ -116,6 +116,10 @@ struct ClassLaunch {
   // the two launches of a class partition their common rows.  nullptr: no test.
   const int* row_split;
   float wthr;
+  // > 0: density screening of every quartet of the launch: quartets with
+  // Q_ab Q_cd max|D| (the same bound) below dskip are skipped (incremental
+  // builds on a density difference)
+  float dskip;
   unsigned long long* counters;  // [0] quartets, [1] primitive quartets computed (nullptr: not counted)
 };
 

@@ -193,13 +193,15 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
     if (active) {
       int row, kloc;
       decode_lane(cl, t, bra, ket, slice, nslice, &row, &kloc, &kslice, &nkslice);
-      if (cl.row_split && kloc < __ldg(cl.row_split + row)) {
-        // density-weighted precision split: this launch keeps its side of the bound
+      const bool split = cl.row_split && kloc < __ldg(cl.row_split + row);
+      if (split || cl.dskip > 0.0f) {
         const PairInfo& Pb = a.pairs[bra];
         const PairInfo& Pk = a.pairs[ket];
-        const float w = quartet_dmax(a, bra, ket, Pb, Pk);
-        const bool heavy = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), w) >= cl.wthr;
-        active = heavy == (sizeof(R) == sizeof(double));
+        const float bound = __fmul_rn(__fmul_rn(Pb.Q, Pk.Q), quartet_dmax(a, bra, ket, Pb, Pk));
+        // density-weighted precision split: this launch keeps its side of the bound
+        if (split) active = (bound >= cl.wthr) == (sizeof(R) == sizeof(double));
+        // density screening (incremental builds on a density difference)
+        if (bound < cl.dskip) active = false;
       }
     } else {
       bra = ket = __ldg(cl.bra_list);

@@ -231,6 +231,8 @@ struct fock_ctx {
   double *d_D = nullptr, *d_M = nullptr, *d_G = nullptr;
   float* d_D32 = nullptr;
   float* d_pair_dmax = nullptr;  // per build: max |D32| of each shell pair's block (mixed split)
+  float dskip = 0.0f;            // > 0: density screening of the builds (see ClassLaunch::dskip)
+  double* h_stage = nullptr;     // pinned host staging of D and G for fock_build_jk (2 n^2, lazily)
   // plans
   std::vector<Plan> plans;
   int* d_plan_int = nullptr;
@@ -617,6 +619,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
     P.p.cl.queue = reinterpret_cast<unsigned long long*>(c->d_plan_ll + c->queue_base + c->plans.size());
     P.p.cl.row_split = c->split_counts ? c->d_plan_int + P.split : nullptr;
     P.p.cl.wthr = (float)c->opt.mixed_threshold;
+    P.p.cl.dskip = for_tensor ? 0.0f : c->dskip;
     P.p.cl.counters = c->split_counts ? reinterpret_cast<unsigned long long*>(
                                             c->d_plan_ll + c->queue_base + pend.size() + 1 + 2 * c->plans.size())
                                       : nullptr;
@@ -625,6 +628,16 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   st.launches_per_build = (int)c->plans.size() + 1;
   if (!for_tensor) c->stats = st;
   return FOCK_OK;
+}
+
+// Density screening threshold of the builds (ClassLaunch::dskip): set in the
+// current plans and in every plan built later; the captured build graph is
+// rebuilt at the next build.
+void set_dskip(fock_ctx* c, float v) {
+  if (c->dskip == v) return;
+  c->dskip = v;
+  for (Plan& p : c->plans) p.cl.dskip = v;
+  if (c->jk_exec) { cudaGraphExecDestroy(c->jk_exec); c->jk_exec = nullptr; }
 }
 
 int compute_schwarz(fock_ctx* c) {
@@ -813,6 +826,7 @@ void fock_ctx_destroy(fock_ctx* c) {
   dfree(c->d_mdfuncs); dfree(c->d_mdexps); dfree(c->d_mdcoefs); dfree(c->d_atoms4); dfree(c->d_func_atom);
   dfree(c->d_mol_off); dfree(c->d_mol_n);
   dfree(c->d_tensor);
+  if (c->h_stage) cudaFreeHost(c->h_stage);
   if (c->blas) cublasDestroy(c->blas);
   if (c->solver) cusolverDnDestroy(c->solver);
   if (c->jk_exec) cudaGraphExecDestroy(c->jk_exec);
@@ -1149,13 +1163,13 @@ static std::vector<int> plan_order(const fock_ctx* c) {
 static cudaError_t issue_jk_build(fock_ctx* c, cudaStream_t cs, int* kernels) {
   const size_t nn = (size_t)c->total_elems;
   EriArgs a = eri_args(c);
-  bool need32 = false;
+  bool need32 = c->dskip > 0.0f;  // the density screening reads the FP32 copy too
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
   const std::vector<int> order = plan_order(c);
   const int nside = std::min<int>(kForkStreams, std::max<size_t>(1, c->plans.size()));
   cudaError_t e = cudaMemsetAsync(c->d_M, 0, nn * sizeof(double), cs);
   if (e == cudaSuccess && need32) { e = k_to_float(c->d_D, c->d_D32, (int)nn, cs); (*kernels)++; }
-  if (e == cudaSuccess && c->split_counts) {
+  if (e == cudaSuccess && (c->split_counts || c->dskip > 0.0f)) {
     e = k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), c->d_D32, c->d_pair_dmax, cs);
     (*kernels)++;
   }
@@ -1228,13 +1242,13 @@ int fockgb_build_jk_scratch(fock_ctx* c, const double* D_dev, double* G_dev, dou
   a.D = D_dev;
   a.D32 = D32;
   a.M = M;
-  bool need32 = false;
+  bool need32 = c->dskip > 0.0f;
   for (const Plan& p : c->plans) need32 |= p.prec == PREC_FP32;
   if (need32) {
     CK(k_to_float(D_dev, D32, (int)nn, cs));
     c->launches++;
   }
-  if (c->split_counts) {
+  if (c->split_counts || c->dskip > 0.0f) {
     CK(k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), D32, c->d_pair_dmax, cs));
     c->launches++;
   }
@@ -1363,7 +1377,7 @@ int fock_profile_build(fock_ctx* c, const double* D_dev, fock_launch_profile* ou
   a.D = D_dev;
   CK(k_to_float(D_dev, c->d_D32, (int)nn, c->stream));
   c->launches++;
-  if (c->split_counts) {
+  if (c->split_counts || c->dskip > 0.0f) {
     CK(k_pair_dmax(c->d_pairs, (int)c->hpairs.size(), c->d_D32, c->d_pair_dmax, c->stream));
     c->launches++;
   }
@@ -1396,14 +1410,17 @@ int fock_build_jk(fock_ctx* c, const double* D, double* G) {
   CK(cudaSetDevice(c->device));
   const int n = c->nbf;
   const size_t nn = (size_t)n * n;
-  std::vector<double> Ds(nn), Gs(nn);
-  to_std(c, D, Ds.data());
-  CK(cudaMemcpyAsync(c->d_D, Ds.data(), nn * 8, cudaMemcpyHostToDevice, c->stream));
+  // D and G pass through pinned staging (sign convention applied there), so
+  // both copies are asynchronous DMA on the context's stream
+  if (!c->h_stage) CK(cudaMallocHost(&c->h_stage, 2 * nn * sizeof(double)));
+  double *Ds = c->h_stage, *Gs = c->h_stage + nn;
+  to_std(c, D, Ds);
+  CK(cudaMemcpyAsync(c->d_D, Ds, nn * 8, cudaMemcpyHostToDevice, c->stream));
   int rc = fock_build_jk_device(c, c->d_D, c->d_G);
   if (rc != FOCK_OK) return rc;
-  CK(cudaMemcpyAsync(Gs.data(), c->d_G, nn * 8, cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaMemcpyAsync(Gs, c->d_G, nn * 8, cudaMemcpyDeviceToHost, c->stream));
   CK(cudaStreamSynchronize(c->stream));
-  to_std(c, Gs.data(), G);
+  to_std(c, Gs, G);
   return FOCK_OK;
 }
 
@@ -2303,12 +2320,38 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     }
   }
 
+  // incremental FP64 refinement of a mixed SCF (as in fock_batch_scf): the
+  // builds after the first FP64 one run on D - D_prev with density screening
+  // and add G_prev
+  const bool incremental = !graph_done && mixed && c->opt.final_fp64 && !refc;
+  double *Gprev = nullptr, *Dprev = nullptr, *Din = nullptr;
+  int* d_one = nullptr;
+  bool had64 = false;  // the previous build was FP64
+  if (incremental && fail == FOCK_OK) {
+    Gprev = mk(nn);
+    Dprev = mk(nn);
+    Din = mk(nn);
+    d_one = reinterpret_cast<int*>(mk(1));
+    if (!Gprev || !Dprev || !Din || !d_one) { cleanup(); return FOCK_ERR_OOM; }
+    const int one_i = 1;
+    cku(cudaMemcpyAsync(d_one, &one_i, sizeof(int), cudaMemcpyHostToDevice, s));
+    cku(cudaStreamSynchronize(s));
+    set_dskip(c, (float)c->opt.schwarz_eps);
+  }
   for (int iter = 0; !graph_done && iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
     auto tp = clk::now();
+    const bool incr = incremental && fp64_phase && had64;
+    if (incr) { cku(kb_incr_input(Dm, Dprev, d_one, c->d_mol_off, 1, (long long)nn, Din, s)); c->launches++; }
     cudaEventRecord(ev0, s);
     if (refc) { cku(md_g_from_tensor(c->d_tensor, Dm, n, G, s)); c->launches++; }
-    else { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
+    else { int r = fock_build_jk_device(c, incr ? Din : Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
+    if (incr) { cku(kb_incr_output(G, Gprev, d_one, c->d_mol_off, 1, (long long)nn, s)); c->launches++; }
+    if (incremental) {
+      cku(cudaMemcpyAsync(Gprev, G, nn * 8, cudaMemcpyDeviceToDevice, s));
+      cku(cudaMemcpyAsync(Dprev, Dm, nn * 8, cudaMemcpyDeviceToDevice, s));
+      had64 = fp64_phase;
+    }
     builds++;
     phase(0, tp);
     cku(k_add(H, G, F, (int)nn, s));
@@ -2388,6 +2431,7 @@ int fock_scf(fock_ctx* c, int charge, fock_scf_result* res) {
     e_prev = e_cur;
     std::swap(Dm, Dn);
   }
+  set_dskip(c, 0.0f);
   if (fp64_phase) fock_set_precision(c, FOCK_PREC_MIXED, mixed_th);
   cudaEventDestroy(ev0);
   cudaEventDestroy(ev1);
@@ -2576,7 +2620,24 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   int* d_order = (int*)mk(ring * sizeof(int));
   int* d_info = (int*)mk((size_t)nmol * sizeof(int));
   long long* d_woff = (long long*)mk((nmol + 1) * sizeof(long long));
-  auto cleanup = [&]() { for (void* p : bufs) cudaFree(p); };
+  // incremental FP64 refinement of a mixed SCF: after a molecule's first FP64
+  // build, its later builds run on D - D_prev and add G_prev (the builds are
+  // linear in D), with density screening, so the refinement's second and later
+  // FP64 builds skip the quartets whose bound Q_ab Q_cd max|D - D_prev| is
+  // below the Schwarz threshold
+  const bool incremental = c->opt.precision == FOCK_PREC_MIXED && c->opt.final_fp64;
+  double *Gprev = nullptr, *Dprev = nullptr, *Din = nullptr;
+  int* d_incr = nullptr;
+  if (incremental) {
+    Gprev = (double*)mk(TB);
+    Dprev = (double*)mk(TB);
+    Din = (double*)mk(TB);
+    d_incr = (int*)mk((size_t)nmol * sizeof(int));
+  }
+  auto cleanup = [&]() {
+    for (void* p : bufs) cudaFree(p);
+    set_dskip(c, 0.0f);  // the context's own builds screen by Schwarz alone
+  };
   if (!ok) { cleanup(); return FOCK_ERR_OOM; }
   int fail = FOCK_OK;
   auto cku = [&](cudaError_t x) { if (x != cudaSuccess && fail == FOCK_OK) fail = map_cuda(x); };
@@ -2782,12 +2843,34 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
     t0 = t1;
   };
   const auto t_loop0 = clk::now();
+  std::vector<int> incr(nmol, 0), was64(nmol, 0);
+  if (incremental) set_dskip(c, (float)c->opt.schwarz_eps);
   for (int iter = 0; iter <= c->opt.max_iters && fail == FOCK_OK; ++iter) {
     const auto ti0 = clk::now();
     auto tp = ti0;
+    bool any_incr = false;
+    if (incremental)
+      for (int k = 0; k < nmol; ++k) {
+        incr[k] = (mode[k] == 2 && was64[k]) ? 1 : 0;
+        any_incr |= incr[k] != 0;
+      }
+    if (any_incr) {
+      cku(cudaMemcpyAsync(d_incr, incr.data(), nmol * sizeof(int), cudaMemcpyHostToDevice, s));
+      cku(kb_incr_input(Dm, Dprev, d_incr, c->d_mol_off, nmol, T, Din, s));
+      c->launches++;
+    }
     cudaEventRecord(ev0, s);
-    { int r = fock_build_jk_device(c, Dm, G); if (r != FOCK_OK) { fail = r; break; } }
+    { int r = fock_build_jk_device(c, any_incr ? Din : Dm, G); if (r != FOCK_OK) { fail = r; break; } }
     cudaEventRecord(ev1, s);
+    if (any_incr) {
+      cku(kb_incr_output(G, Gprev, d_incr, c->d_mol_off, nmol, T, s));
+      c->launches++;
+    }
+    if (incremental) {
+      cku(cudaMemcpyAsync(Gprev, G, TB, cudaMemcpyDeviceToDevice, s));
+      cku(cudaMemcpyAsync(Dprev, Dm, TB, cudaMemcpyDeviceToDevice, s));
+      for (int k = 0; k < nmol; ++k) was64[k] = mode[k] == 2 ? 1 : 0;
+    }
     builds++;
     phase(0, tp);
     cku(k_add(H, G, F, (int)T, s));
@@ -2890,6 +2973,7 @@ int fock_batch_scf(fock_batch* b, const int* charges, fock_scf_result* results) 
   if (trace)
     std::fprintf(stderr, "fock_batch_scf: phases: build %.3f s, F/DIIS %.3f s, shift+density %.3f s\n", t_ph[0],
                  t_ph[1], t_ph[2]);
+  set_dskip(c, 0.0f);
   if (replans) {  // back to the context's own plan
     c->mol_mode.clear();
     int r = build_plan(c, false);

@@ -517,6 +517,32 @@ cudaError_t kb_guess(const double* S, const double* H, const long long* off, con
   return cudaGetLastError();
 }
 
+// Incremental Fock builds (G(D) = G(D_prev) + G(D - D_prev), linear in D):
+// the build input of block m is D - D_prev where incr[m], else D; the
+// result of an incremental block then adds G_prev.
+__global__ void incr_input_kernel(const double* D, const double* Dprev, const int* incr, const long long* off,
+                                  int nmol, long long total, double* Din) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  Din[t] = incr[block_of(off, nmol, t)] ? D[t] - Dprev[t] : D[t];
+}
+__global__ void incr_output_kernel(double* G, const double* Gprev, const int* incr, const long long* off, int nmol,
+                                   long long total) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= total) return;
+  if (incr[block_of(off, nmol, t)]) G[t] += Gprev[t];
+}
+cudaError_t kb_incr_input(const double* D, const double* Dprev, const int* incr, const long long* off, int nmol,
+                          long long total, double* Din, cudaStream_t s) {
+  incr_input_kernel<<<nblk(total, 256), 256, 0, s>>>(D, Dprev, incr, off, nmol, total, Din);
+  return cudaGetLastError();
+}
+cudaError_t kb_incr_output(double* G, const double* Gprev, const int* incr, const long long* off, int nmol,
+                           long long total, cudaStream_t s) {
+  incr_output_kernel<<<nblk(total, 256), 256, 0, s>>>(G, Gprev, incr, off, nmol, total);
+  return cudaGetLastError();
+}
+
 
 // ---------------------------------------------------------------------------
 // Device-driven RHF loop (see ScfDevState): the host loop of fock_scf

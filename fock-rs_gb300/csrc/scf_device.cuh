@@ -43,6 +43,11 @@ cudaError_t kb_diis_extrapolate(const double* Fring, long long total, const int*
                                 int ring, int last, const long long* off, int nmol, double* Fd, cudaStream_t s);
 cudaError_t kb_scale_cols(const double* U, const double* w, const long long* woff, const long long* off,
                           const int* n, int nmol, long long total, double* W, cudaStream_t s);
+// incremental builds: Din = incr[m] ? D - Dprev : D per block; G += incr[m] ? Gprev : 0
+cudaError_t kb_incr_input(const double* D, const double* Dprev, const int* incr, const long long* off, int nmol,
+                          long long total, double* Din, cudaStream_t s);
+cudaError_t kb_incr_output(double* G, const double* Gprev, const int* incr, const long long* off, int nmol,
+                           long long total, cudaStream_t s);
 cudaError_t kb_guess(const double* S, const double* H, const long long* off, const int* n, int nmol, long long total,
                      int gwh, double* F, cudaStream_t s);
 }  // namespace fockgb

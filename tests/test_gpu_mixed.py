@@ -82,3 +82,26 @@ def test_fp32_integral_error(gpu_lib):
     # the mixed tensor keeps Q_ab Q_cd >= threshold in FP64: far smaller errors
     tmx = ElectronTensor.from_basis(atoms, precision=L.FOCK_PREC_MIXED, mixed_threshold=1e-3).data
     assert np.abs(tmx - t64).max() < 0.1 * err.max()
+
+
+def test_mixed_scf_incremental_refinement_host_loop(gpu_lib):
+    """(H2O)8 / 6-31G* (152 functions: the host-driven SCF loop): the mixed SCF
+    finishes with FP64 builds, the second and later of them incremental (on
+    D - D_prev, density-screened); the converged energy equals the plain FP64
+    SCF's to 1e-9 Eh."""
+    Zs, xyz = M.water_cluster(8, seed=0)
+    atoms = B.build_atoms("6-31G*", Zs, xyz)
+    kw = dict(guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY, energy_mode=1, epsilon=1e-10, max_iters=100,
+              sign_convention=L.FOCK_SIGN_STANDARD)
+    energies = {}
+    for prec in (L.FOCK_PREC_FP64, L.FOCK_PREC_MIXED):
+        with FockContext(atoms, precision=prec, **kw) as c:
+            rc, r, _, _, _ = c.scf(0)
+            assert rc == 0 and r.converged
+            energies[prec] = r.total_energy
+            # the context's own plan is back: a build equals a fresh context's
+            D = random_density(c.n, seed=3, nocc=40)
+            G = c.build_jk(D)
+        with FockContext(atoms, precision=prec, **kw) as fresh:
+            assert np.abs(fresh.build_jk(D) - G).max() < 1e-12
+    assert abs(energies[L.FOCK_PREC_MIXED] - energies[L.FOCK_PREC_FP64]) < 1e-9, energies
