@@ -171,12 +171,18 @@ __device__ __forceinline__ double f2d_exact(float f) {
 // Householder iteration for x^{-1/2}; see Muller et al., Handbook of
 // Floating-Point Arithmetic, ch. 5).  Seed error ~1e-7 -> ~1e-20 + rounding.
 __device__ __forceinline__ double rsqrt_fp64(double x) {
-  double y = (double)rsqrtf(approx_float(x));
+  double y = f2d_exact(rsqrtf(approx_float(x)));  // the seed widened by integer operations
   double t = x * y;
   double e = fma(-t, y, 1.0);
   double c = fma(e, 0.375, 0.5);
   // seed error ~2^-20 (approx_float) -> cubic step leaves ~1e-18
   return fma(y * e, c, y);
+}
+
+// x / 2 for a normal double well above the underflow threshold, by
+// decrementing its exponent (an integer operation, no FP64-pipe multiply).
+__device__ __forceinline__ double half_of(double x) {
+  return __hiloint2double(__double2hiint(x) - (1 << 20), __double2loint(x));
 }
 
 // Component normalisation relative to the x^l component: the reference
@@ -252,17 +258,17 @@ __device__ __forceinline__ void boys_scaled(double T, double pref, const double*
       e = fma(e, nd, 0.5);
       e = fma(e, nd, 1.0);
       e = fma(e, nd, 1.0);
-      e *= ex;
+      // the recursion runs on pref-scaled values (it is linear in F and e^{-T}):
+      // two multiplies by pref instead of L + 1
+      e *= ex * pref;
       const double t2 = T + T;
-      F[L] = f;
+      F[L] = f * pref;
 #pragma unroll
       for (int m = L; m > 0; --m) F[m - 1] = fma(t2, F[m], e) * (1.0 / (2 * m - 1));
-#pragma unroll
-      for (int m = 0; m <= L; ++m) F[m] *= pref;
     }
   } else {
     const double r = rsqrt_fp64(T);
-    const double inv2t = 0.5 * r * r;
+    const double inv2t = half_of(r * r);  // 1/(2T); 1/T >= 1e-30 here, far from underflow
     double f = 0.88622692545275801365 * r * pref;  // sqrt(pi)/2
     F[0] = f;
 #pragma unroll
