@@ -312,6 +312,8 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
         t = _event_times(torch, stream, lambda: ctx.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
         ms = sum(t) / len(t)
         out[name] = {"ms_per_build": ms, "quartets_per_s": nq / (ms * 1e-3)}
+        if prec == L.FOCK_PREC_FP64:  # model FP64 flops of the plan over the build time
+            out[name]["tflops_fp64"] = ctx.stats()["flops_fp64"] / (ms * 1e-3) / 1e12
         Gs[name] = G.clone()
     out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_build"] / out["mixed"]["ms_per_build"]
     out["mixed"]["single_build_energy_error_eh"] = abs(0.5 * float((D * (Gs["mixed"] - Gs["fp64"])).sum().item()))
