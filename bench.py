@@ -317,6 +317,18 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
         Gs[name] = G.clone()
     out["mixed"]["speedup_vs_fp64"] = out["fp64"]["ms_per_build"] / out["mixed"]["ms_per_build"]
     out["mixed"]["single_build_energy_error_eh"] = abs(0.5 * float((D * (Gs["mixed"] - Gs["fp64"])).sum().item()))
+    # launch parameters of the mixed build chosen by the autotuner (fresh cache):
+    # slicing, block size and persistent (work-queue) launches
+    import tempfile
+    from fock_gb300.tuning import autotune
+    with tempfile.TemporaryDirectory() as td:
+        tuned = autotune(ctx, D.data_ptr(), reps=2, cache_path=os.path.join(td, "tune.json"))
+    t = _event_times(torch, stream, lambda: ctx.build_jk_device(D.data_ptr(), G.data_ptr()), steps, warmup, flush)
+    ms_t = sum(t) / len(t)
+    out["mixed_autotuned"] = {"ms_per_build": ms_t, "quartets_per_s": nq / (ms_t * 1e-3),
+                              "speedup_vs_fp64": out["fp64"]["ms_per_build"] / ms_t,
+                              "tuning": {k: tuned[k] for k in ("prims_per_slice", "prims_per_slice_fp32",
+                                                               "block_threads", "persistent")}}
     ctx.close()
     if builds_only:
         return out
