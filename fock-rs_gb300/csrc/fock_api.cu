@@ -188,13 +188,13 @@ struct CatSeg {
 };
 struct CatGroup {  // one launch group: bra class, ket class, ket primitive-pair count
   int la, lb, lc, ld;
-  int key;  // primitive pairs of every ket of the group (-1: mixed counts)
+  int key;  // grouping key shared by every ket of the group (-1: no grouping)
   std::vector<CatSeg> segs;
 };
 struct PlanCatalog {
   bool valid = false;
   double tau = -1.0, tmix = -1.0;
-  bool grouping = true;
+  int grouping = 1;
   std::vector<CatGroup> groups;
   std::vector<int> kets;        // ket pair ids, segment after segment
   std::vector<long long> kpre;  // kpre[i] = primitive pairs of kets[0..i)
@@ -217,6 +217,7 @@ struct fock_ctx {
   // pairs
   std::vector<PairInfo> hpairs;
   std::vector<int> pair_nprim;
+  std::vector<int> pair_sig;  // exponent signature of each pair (equal primitive exponent sums, in order)
   long long nprim_pairs = 0;
   PairInfo* d_pairs = nullptr;
   PrimPair64* d_prim64 = nullptr;
@@ -334,7 +335,7 @@ int class_vrr_flops(int la, int lb, int lc, int ld, int* hrr, int* neri);
 // threshold, grouping) and re-assembled into launch plans by build_plan, so
 // that the batched SCF can drop converged molecules or move molecules to FP64
 // without redoing the per-row searches.
-static void build_catalog(const fock_ctx* c, double tau, double tmix, bool grouping, PlanCatalog& cat) {
+static void build_catalog(const fock_ctx* c, double tau, double tmix, int grouping, PlanCatalog& cat) {
   cat = PlanCatalog();
   cat.tau = tau;
   cat.tmix = tmix;
@@ -375,11 +376,14 @@ static void build_catalog(const fock_ctx* c, double tau, double tmix, bool group
           if (pair_class(a, b) == X) { la = a; lb = b; }
           if (pair_class(a, b) == Y) { lc = a; ld = b; }
         }
-      // ket groups by primitive-pair count (uniform inner loops); -1 = all
+      // ket groups (uniform inner loops): by primitive-pair count (1) or by
+      // exponent signature (2: the same exponents in the same order, so a
+      // warp's lanes share every primitive's exponent sum); -1 = all
+      auto key_of = [&](int p) { return grouping == 2 ? c->pair_sig[p] : c->hpairs[p].nprim; };
       std::vector<int> keys;
       if (grouping) {
         for (int m = 0; m < nmol; ++m)
-          for (int p : cls[m][Y]) keys.push_back(c->hpairs[p].nprim);
+          for (int p : cls[m][Y]) keys.push_back(key_of(p));
         std::sort(keys.begin(), keys.end());
         keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
       } else {
@@ -394,7 +398,7 @@ static void build_catalog(const fock_ctx* c, double tau, double tmix, bool group
           if (bras.empty() || cls[m][Y].empty()) continue;
           g.clear();  // this molecule's kets of the group, Q order
           for (int p : cls[m][Y])
-            if (key < 0 || c->hpairs[p].nprim == key) g.push_back(p);
+            if (key < 0 || key_of(p) == key) g.push_back(p);
           if (g.empty()) continue;
           gq.resize(g.size());
           grank.resize(g.size());
@@ -454,7 +458,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   // quartets whose bound can reach the threshold with max|D| <= kDensityPlanMax
   const bool density = !for_tensor && c->opt.mixed_density != 0;
   const double tmix = density ? c->opt.mixed_threshold / kDensityPlanMax : c->opt.mixed_threshold;
-  const bool grouping = c->opt.group_by_contraction != 0;
+  const int grouping = std::max(0, std::min(2, c->opt.group_by_contraction));
   PlanCatalog tensor_cat;
   if (for_tensor) {
     build_catalog(c, tau, tmix, grouping, tensor_cat);
@@ -739,7 +743,7 @@ void fock_options_default(fock_options* o) {
   o->schwarz_eps = 1e-12;
   o->mixed_threshold = 1.0;
   o->prim_eps = 1e-20;
-  o->group_by_contraction = 1;
+  o->group_by_contraction = 2;
   o->max_iters = 100;
   o->epsilon = 1e-6;
   o->conv_mode = FOCK_CONV_COMMUTATOR;
@@ -1014,6 +1018,21 @@ int create_ctx(const fock_atom* atoms, int natom, const fock_shell* shells, int 
     float idf;
     std::memcpy(&idf, &idi, sizeof(idf));
     p32[k].v[2].y = idf;
+  }
+  {  // exponent signatures: pairs whose primitive pairs have the same exponent sums in the same order
+    std::map<std::vector<int>, int> sig_id;
+    c->pair_sig.assign(c->hpairs.size(), 0);
+    for (size_t q = 0; q < c->hpairs.size(); ++q) {
+      const PairInfo& P = c->hpairs[q];
+      std::vector<int> sig;
+      for (int k = 0; k < P.nprim; ++k) {
+        long long id;
+        std::memcpy(&id, &p64[P.prim_off + k].v[4].y, sizeof(id));
+        sig.push_back((int)id);
+      }
+      auto it = sig_id.emplace(std::move(sig), (int)sig_id.size()).first;
+      c->pair_sig[q] = it->second;
+    }
   }
   // in double: each entry within about one ulp (long double is a software
   // quad type on Arm hosts, where this table took milliseconds per context)

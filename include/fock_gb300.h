@@ -82,7 +82,9 @@ typedef struct {
   double schwarz_eps;     /* shell-quartet screening: skip Q_ab Q_cd < schwarz_eps (exact mode) */
   double mixed_threshold; /* FOCK_PREC_MIXED: FP64 for Q_ab Q_cd >= mixed_threshold */
   double prim_eps;        /* drop primitive pairs with |K_ab| below this */
-  int group_by_contraction; /* split ket lists by primitive-pair count (uniform warps) */
+  int group_by_contraction; /* split ket lists into groups of uniform inner loops: 0 none, 1 by
+                               primitive-pair count, 2 by exponent signature (equal primitive
+                               exponent sums in the same order) */
   /* SCF */
   int max_iters;
   double epsilon;

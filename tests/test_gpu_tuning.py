@@ -32,7 +32,7 @@ def reference_g(mol):
 @pytest.mark.parametrize("kw", [dict(persistent=1), dict(block_threads=64), dict(block_threads=256),
                                 dict(prims_per_slice=4), dict(prims_per_slice=2, persistent=1, block_threads=256),
                                 dict(group_by_contraction=0), dict(prims_per_slice=-16, prims_per_slice_fp32=-32),
-                                dict(prims_per_slice=-8, group_by_contraction=0)])
+                                dict(prims_per_slice=-8, group_by_contraction=0), dict(group_by_contraction=1)])
 def test_launch_parameters_keep_g(gpu_lib, mol, reference_g, kw):
     D, G0 = reference_g
     with FockContext(mol, **kw) as ctx:
