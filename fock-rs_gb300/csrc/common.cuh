@@ -8,10 +8,18 @@ namespace fockgb {
 // ---------------------------------------------------------------------------
 // Boys-function tables.
 // F_n(T) is tabulated on T_i = i/32, i = 0..2048 (T < 64).  For every order M
-// a 64-byte row holds the Taylor coefficients c_k = F_{M+k}(T_i) (-1)^k / k!,
-// k = 0..6, and exp(-T_i) in slot 7, so that with d = T - T_i, |d| <= 1/64,
-//   F_M(T) = sum_k c_k d^k          (truncation (1/64)^7/7! < 5e-17 relative)
-//   e^{-T} = e^{-T_i} sum_k (-d)^k/k!, k <= 6 (same bound)
+// a 64-byte row holds six polynomial coefficients in slots 0..5 and exp(-T_i)
+// in slot 7 (slot 6 is zero), so that with d = T - T_i, |d| <= h = 1/64,
+//   F_M(T) = sum_{k<=5} c'_k d^k
+// where c'_k are the Taylor coefficients c_k = F_{M+k}(T_i) (-1)^k / k! with
+// the degree-6 term Chebyshev-economised into the even ones (Press et al.,
+// Numerical Recipes, 5.11): on |d| <= h, d^6 = h^6 T_6(d/h)/32 + (3/2) h^2 d^4
+// - (9/16) h^4 d^2 + h^6/32, so c'_4 = c_4 + (3/2) h^2 c_6,
+// c'_2 = c_2 - (9/16) h^4 c_6, c'_0 = c_0 + h^6 c_6 / 32.  The dropped term is
+// at most c_6 h^6/32 + |c_7| h^7 < 1e-16 relative (6e-16 measured against
+// 40-digit values for orders 0..12, with double rounding), one FMA per row
+// fewer than the degree-6 Taylor polynomial.
+//   e^{-T} = e^{-T_i} sum_k (-d)^k/k!, k <= 6 (truncation (1/64)^7/7! < 5e-17)
 // and lower orders follow by the downward recursion
 //   F_{m-1} = (2T F_m + e^{-T}) / (2m - 1).
 // For T >= 64, F_0 = sqrt(pi/T)/2 and F_m = F_{m-1} (2m-1)/(2T) (the neglected
@@ -19,8 +27,9 @@ namespace fockgb {
 // ---------------------------------------------------------------------------
 constexpr int kBoysPerUnit = 32;
 constexpr int kBoysPts = 64 * kBoysPerUnit + 1;
-constexpr int kBoysTerms = 8;           // 7 Taylor coefficients + exp(-T_i)
-constexpr int kBoysTaylor = 7;
+constexpr int kBoysTerms = 8;           // 6 coefficients, 0, exp(-T_i)
+constexpr int kBoysTaylor = 7;          // Taylor terms before the economisation
+constexpr int kBoysPoly = 6;            // coefficients evaluated
 constexpr int kBoysMaxM = 12;           // orders with a Taylor table
 // FP32 table: 16-byte rows of the first four coefficients (cubic Taylor
 // polynomial, truncation (1/64)^4/4! < 3e-9 relative), half the footprint of
@@ -208,8 +217,7 @@ __host__ __device__ __forceinline__ double comp_factor(int l, int c) {
 __device__ __forceinline__ double boys_taylor_row(const double* __restrict__ row, double d, double* ex) {
   const double2* r2 = reinterpret_cast<const double2*>(row);
   const double2 c01 = __ldg(r2), c23 = __ldg(r2 + 1), c45 = __ldg(r2 + 2), c6e = __ldg(r2 + 3);
-  double f = fma(c6e.x, d, c45.y);
-  f = fma(f, d, c45.x);
+  double f = fma(c45.y, d, c45.x);
   f = fma(f, d, c23.y);
   f = fma(f, d, c23.x);
   f = fma(f, d, c01.y);

@@ -112,17 +112,23 @@ void build_tables() {
   g_boys32.assign((size_t)(kBoysMaxM + 1) * kBoysPts * kBoysTerms32, 0.0f);
   for (int M = 0; M <= kBoysMaxM; ++M)
     for (int i = 0; i < kBoysPts; ++i) {
-      long double fact = 1.0L;
+      long double fact = 1.0L, c[kBoysTaylor];
       const size_t row = ((size_t)M * kBoysPts + i) * kBoysTerms;
       for (int k = 0; k < kBoysTaylor; ++k) {
         if (k > 0) fact *= k;
-        long double c = F[(size_t)i * (kTabOrders + 1) + M + k] / fact;
-        if (k & 1) c = -c;
-        g_boys64[row + k] = (double)c;
-        if (k < kBoysTerms32) g_boys32[((size_t)M * kBoysPts + i) * kBoysTerms32 + k] = (float)c;
+        c[k] = F[(size_t)i * (kTabOrders + 1) + M + k] / fact;
+        if (k & 1) c[k] = -c[k];
+        if (k < kBoysTerms32) g_boys32[((size_t)M * kBoysPts + i) * kBoysTerms32 + k] = (float)c[k];
       }
+      // the degree-6 term economised into c_0, c_2, c_4 on |d| <= h (see common.cuh)
+      static_assert(kBoysTaylor == 7 && kBoysPoly == 6, "economisation of the degree-6 term");
+      const long double h = 0.5L / kBoysPerUnit, h2 = h * h;
+      c[4] += 1.5L * h2 * c[6];
+      c[2] -= 0.5625L * h2 * h2 * c[6];
+      c[0] += h2 * h2 * h2 * c[6] / 32.0L;
+      for (int k = 0; k < kBoysPoly; ++k) g_boys64[row + k] = (double)c[k];
       const long double ex = expl(-(long double)i / (long double)kBoysPerUnit);
-      g_boys64[row + kBoysTaylor] = (double)ex;
+      g_boys64[row + kBoysTerms - 1] = (double)ex;
     }
   // reference LUT: F_10(0.15 k), k < 200, the values stored in boys/src/lut.rs
   g_ref_lut.assign(kRefBoysLut, kRefBoysLut + 200);
@@ -313,8 +319,8 @@ MdTables md_tables(fock_ctx* c) {
 // the kernel evaluates them: PQ (3), |PQ|^2 (5), T = p (rho/p) |PQ|^2 (2),
 // prefactor (2), WP and WQ when the bra / ket carries angular momentum (3
 // each), 1/(2(p+q)) when both do, the table offset d (2) and the Boys
-// function: per order a 7-term Horner (12) and the prefactor (1) for L <= 1;
-// otherwise one Horner (12), e^{-T} (11), 2T (1), the downward recursion
+// function: per order a 6-term Horner (10) and the prefactor (1) for L <= 1;
+// otherwise one Horner (10), e^{-T} (11), 2T (1), the downward recursion
 // (3 per order) and the prefactors (L + 1).  The exponent-sum quantities
 // come from a table (no flops).
 long long setup_flops(int la, int lb, int lc, int ld) {
@@ -323,8 +329,8 @@ long long setup_flops(int la, int lb, int lc, int ld) {
   if (la + lb > 0) f += 3;
   if (lc + ld > 0) f += 3;
   if (la + lb > 0 && lc + ld > 0) f += 1;
-  if (L <= 1) f += (L + 1) * 13;
-  else f += 12 + 11 + 1 + 3LL * L + (L + 1);
+  if (L <= 1) f += (L + 1) * 11;
+  else f += 10 + 11 + 1 + 3LL * L + (L + 1);
   return f;
 }
 

@@ -55,8 +55,8 @@ __device__ void boys_exact_all(double T, int nmax, const double* __restrict__ ta
     i = i > kBoysPts - 1 ? kBoysPts - 1 : (i < 0 ? 0 : i);
     const double d = T - (double)i / kBoysPerUnit;
     const double* row = tab + ((size_t)nmax * kBoysPts + i) * kBoysTerms;
-    double f = row[kBoysTaylor - 1];
-    for (int k = kBoysTaylor - 2; k >= 0; --k) f = fma(f, d, row[k]);
+    double f = row[kBoysPoly - 1];
+    for (int k = kBoysPoly - 2; k >= 0; --k) f = fma(f, d, row[k]);
     F[nmax] = f;
     if (nmax > 0) {
       const double nd = -d;
