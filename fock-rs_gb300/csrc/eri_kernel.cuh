@@ -456,11 +456,33 @@ __device__ __forceinline__ void eri_lane(const ClassLaunch& cl, const EriArgs& a
   }
 }
 
-// Resident blocks of kEriMaxThreads asked of the compiler: the s/p classes
-// are latency-bound on their gathers (pair data, exponent-sum table, Boys rows)
-// and gain from more warps per SM, i.e. at most 64 registers a thread.
+// Resident blocks of kEriMaxThreads asked of the compiler.  FP64 lanes:
+// FOCK_MINBLOCKS for the classes with L <= FOCK_MINBLOCKS_LMAX (default 1, no
+// bound: the FP64 kernels are bound by their pipe, and bounds of 3-4 blocks
+// measured within +-4 %).  FP32 lanes: resident blocks of kEriMaxThreads asked of the compiler by the
+// class's total angular momentum L.  Without a bound the J/K digestion of the
+// p and d classes holds 88-250 registers a thread, which leaves few warps to
+// hide the lanes' gather latency.  At 4 blocks (64 registers) for L <= 2 and
+// 3 blocks (80 registers) for L = 3 the classes spill at most 32 bytes.
+// Measured: 512-cluster 6-31G mixed batch build 37.2 -> 34.8 ms, (H2O)32
+// 6-31G* mixed build 16.5 -> 15.4 ms (3 blocks for L <= 2: 35.6 and 15.3 ms);
+// bounding the L = 4 classes as well (2 blocks, 128 registers, 50-390 bytes
+// of spills) gained nothing more.
+#ifndef FOCK_MINBLOCKS32_L2
+#define FOCK_MINBLOCKS32_L2 4  // L <= 2
+#endif
+#ifndef FOCK_MINBLOCKS32_L3
+#define FOCK_MINBLOCKS32_L3 3  // L == 3
+#endif
+#ifndef FOCK_MINBLOCKS32_L4
+#define FOCK_MINBLOCKS32_L4 1  // L >= 4
+#endif
 template <class C, typename R>
-constexpr int eri_min_blocks() { return (C::L <= FOCK_MINBLOCKS_LMAX) ? FOCK_MINBLOCKS : 1; }
+constexpr int eri_min_blocks() {
+  return sizeof(R) == sizeof(float)
+             ? (C::L <= 2 ? FOCK_MINBLOCKS32_L2 : C::L == 3 ? FOCK_MINBLOCKS32_L3 : FOCK_MINBLOCKS32_L4)
+             : (C::L <= FOCK_MINBLOCKS_LMAX) ? FOCK_MINBLOCKS : 1;
+}
 
 template <class C, typename R, int MODE>
 __global__ void __launch_bounds__(kEriMaxThreads, (eri_min_blocks<C, R>())) eri_kernel(const ClassLaunch cl, const EriArgs a) {
