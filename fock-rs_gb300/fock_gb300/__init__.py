@@ -15,10 +15,15 @@ reads the same:
 Every call goes through the C ABI (libfock_gb300.so) to the sm_103a kernels.
 """
 import ctypes as C
+import os
 from dataclasses import dataclass
 from typing import List, Optional, Sequence
 
 import numpy as np
+
+# 32 hardware work queues for the CUDA context (a Fock build is a graph of up
+# to 32 parallel class launches): effective when no CUDA context exists yet
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 from . import _lib
 from ._lib import FockError, check, lib

@@ -19,6 +19,13 @@
  *
  * Threading: one context per host thread; calls on one context run in order
  * on its CUDA stream and return after the result is on the host.
+ *
+ * Environment: at load the library sets CUDA_DEVICE_MAX_CONNECTIONS=32 unless
+ * the process has set it (a Fock build is a CUDA graph of up to 32 parallel
+ * class launches; with the default 8 hardware queues some of them can run one
+ * after another).  It applies only to a CUDA context created after the load:
+ * a caller that creates its context first (e.g. through PyTorch) sets it
+ * before doing so.
  */
 #ifndef FOCK_GB300_H
 #define FOCK_GB300_H
