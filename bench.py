@@ -48,7 +48,7 @@ UNIT = "quartets/s"
 SCF_GUESS_NAME = "sad"
 BATCH_LEVEL_SHIFT = 0.0  # Eh
 MIXED_CURVE = (1.0, 0.1, 0.01, 1e-3, 1e-4)  # mixed thresholds of the batch's speed / accuracy curve
-BUILD_DRAM_BYTES_NCU = 4.7e6  # DRAM bytes per benzene FP64 build under ncu (launch list: 4 builds / 4)
+BUILD_DRAM_BYTES_NCU = 5.1e6  # DRAM bytes per benzene FP64 build under ncu (launch list: 4 builds / 4)
 WORKLOAD = {"workload": "C6H6 RHF/6-31G integral-direct Fock build (G = J - K/2)", "molecule": "benzene D6h",
             "basis": "6-31G", "n_basis": 66, "unique_quartets": 2445366, "l2": "flushed between steps (256 MB write)"}
 
@@ -337,6 +337,12 @@ def water32_workload(torch, F, L, local, flush, steps=3, warmup=3, builds_only=F
     ctx.close()
     if builds_only:
         return out
+    # warm-up: a one-iteration SCF of the cluster pays the process's one-time costs
+    # of the first large-basis SCF (cuSOLVER loading at n = 608, the atomic
+    # densities of O and H in 6-31G*) outside the timed SCFs below
+    with F.FockContext(atoms, precision=L.FOCK_PREC_FP64, guess=L.FOCK_GUESS_SAD, max_iters=1,
+                       device=local) as wctx:
+        wctx.scf(0)
     # mixed-precision SCF (final iterations FP64) and the nuclear gradient: analytic
     # derivative kernels for the s/p classes, finite-difference kernels for the d classes
     with F.FockContext(atoms, precision=L.FOCK_PREC_MIXED, guess=L.FOCK_GUESS_SAD, conv_mode=L.FOCK_CONV_ENERGY,
