@@ -156,3 +156,21 @@ def test_header_is_plain_c_and_links(gpu_lib, tmp_path):
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert out.returncode == 0 and out.stdout.split() == ["16", "5", "1"]
+
+
+@pytest.mark.parametrize("preset,expect", [(None, "32"), ("4", "4")])
+def test_library_load_sets_hardware_queue_default(gpu_lib, preset, expect):
+    """Loading the library sets CUDA_DEVICE_MAX_CONNECTIONS=32 for the process
+    unless the caller has set it (checked in a child process, through the C
+    environment, before any CUDA context exists)."""
+    import subprocess
+    import sys
+    from fock_gb300 import _lib as L
+    code = ("import ctypes as C; C.CDLL(%r); libc = C.CDLL(None); libc.getenv.restype = C.c_char_p; "
+            "v = libc.getenv(b'CUDA_DEVICE_MAX_CONNECTIONS'); print(v.decode() if v else '')" % L.LIB_PATH)
+    env = {k: v for k, v in os.environ.items() if k != "CUDA_DEVICE_MAX_CONNECTIONS"}
+    if preset is not None:
+        env["CUDA_DEVICE_MAX_CONNECTIONS"] = preset
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == expect
