@@ -3,7 +3,8 @@
 // Work mapping (MODE_JK / MODE_TENSOR): one lane = one contracted shell
 // quartet and one slice of its bra primitive pairs; lanes are packed densely
 // over the rows of a launch (see ClassLaunch), so a warp's 32 lanes usually
-// share one bra pair and its ket primitive-pair count.  Every lane runs
+// share one bra pair and the exponents of their kets' primitive pairs (kets
+// are grouped by exponent signature).  Every lane runs
 // Obara-Saika VRR over its bra x ket primitive pairs into contracted [e0|f0]
 // accumulators held in registers, then HRR once, then digests the integrals
 // straight into the Fock accumulator M (G = M + M^T) with FP64 atomics: the

@@ -203,9 +203,10 @@ struct CatSeg {
   long long row0;  // first row in PlanCatalog::rbra / rall / r64
   int nrow;
 };
-struct CatGroup {  // one launch group: bra class, ket class, ket primitive-pair count
+struct CatGroup {  // one launch group: bra class, ket class, ket grouping key
   int la, lb, lc, ld;
-  int key;  // grouping key shared by every ket of the group (-1: no grouping)
+  int key;  // shared by every ket of the group: primitive-pair count (grouping 1) or exponent
+            // signature (grouping 2); -1: no grouping
   std::vector<CatSeg> segs;
 };
 struct PlanCatalog {
@@ -506,7 +507,7 @@ int build_plan(fock_ctx* c, bool for_tensor) {
   st.function_quartets_unique = cat.function_quartets_unique;
   std::vector<int> rbra, rbeg, rcnt, kets, rsl, rks, rsplit;
   // one launch per class and precision: the catalog's groups of a class (one
-  // per ket primitive-pair count, adjacent in the catalog) are concatenated,
+  // per ket grouping key, adjacent in the catalog) are concatenated,
   // so a warp mixes trip counts only where two groups meet
   for (size_t g0 = 0; g0 < cat.groups.size();) {
     size_t g1 = g0 + 1;
