@@ -1334,7 +1334,8 @@ extern "C" {
 
 // Autotuner: coordinate search over the launch parameters of the current
 // precision plan, each candidate re-planned, captured and timed with CUDA
-// events over `reps` builds after one warm-up build.
+// events over `reps` builds after one warm-up build; the winner replaces the
+// starting configuration only if it is faster again in a confirmation run.
 int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best) {
   if (!c || !D_dev || !best) return FOCK_ERR_INVALID_ARG;
   CK(cudaSetDevice(c->device));
@@ -1364,6 +1365,7 @@ int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best)
     c->opt.persistent = t.persistent;
   };
   int rc = measure(&cur.ms);
+  const fock_tuning start = cur;
   const std::vector<int> pps64 = {1, 2, 4, -8, -16, -32}, pps32 = {1, 4, -16, -32, -64, -128, -256}, blk = {64, 128, 256},
                          per = {0, 1};
   for (int dim = 0; dim < 4 && rc == FOCK_OK; ++dim) {
@@ -1381,6 +1383,32 @@ int fock_autotune(fock_ctx* c, const double* D_dev, int reps, fock_tuning* best)
       if (t.ms < cur.ms) cur = t;
     }
     apply(cur);
+  }
+  // confirmation: the search ranks candidates on short runs, so its winner is
+  // timed again against the starting configuration (alternating, twice each)
+  // and kept only if it is still the faster one
+  const bool moved = cur.prims_per_slice != start.prims_per_slice ||
+                     cur.prims_per_slice_fp32 != start.prims_per_slice_fp32 ||
+                     cur.block_threads != start.block_threads || cur.persistent != start.persistent;
+  if (rc == FOCK_OK && moved) {
+    float ms_start = 0.f, ms_cur = 0.f, m = 0.f;
+    for (int k = 0; k < 2 && rc == FOCK_OK; ++k) {
+      apply(start);
+      rc = measure(&m);
+      ms_start += m;
+      if (rc != FOCK_OK) break;
+      apply(cur);
+      rc = measure(&m);
+      ms_cur += m;
+    }
+    if (rc == FOCK_OK) {
+      if (ms_start <= ms_cur) {
+        cur = start;
+        cur.ms = 0.5f * ms_start;
+      } else {
+        cur.ms = 0.5f * ms_cur;
+      }
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);

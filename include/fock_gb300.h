@@ -339,7 +339,9 @@ int fock_batch_scf(fock_batch* batch, const int* charges, fock_scf_result* resul
  * "primitives per thread"), threads per block ("quartets per block") and
  * persistent work-queue launches -- chosen by a coordinate search, each
  * candidate timed with CUDA events over `reps` builds of the density D_dev
- * (device, textbook sign).  The best setting stays in the context. */
+ * (device, textbook sign); the search's winner replaces the starting setting
+ * only if a confirmation run (both timed again, alternating) finds it faster.
+ * The chosen setting stays in the context. */
 typedef struct {
   int prims_per_slice, prims_per_slice_fp32, block_threads, persistent;
   float ms; /* time of one build with this setting */
